@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Lanczos steps/s on GB300: Heisenberg chain L=28, periodic, J=1, Sz=0
+(dim 40,116,600), 200 Lanczos steps per run.
+
+One bench step is one complete ground-state run of 200 Lanczos steps in the
+mixed form (FP32 vectors and SpMV, compensated FP64-accurate reductions,
+selective reorthogonalisation, FP64 Rayleigh-quotient/residual refinement),
+from a seeded Gaussian start vector generated on the device.  `value` =
+Lanczos steps/s over the K timed runs (all ranks); `e2e` = the same through the
+C ABI with the start vector and the Ritz vector in pinned host memory.  The
+plain FP64 path (reference semantics: full reorthogonalisation) is run once
+on the same seed for |dE0|; the CPU baseline is the oracle port of the
+reference algorithm (host CSR + CSR SpMV + full reorthogonalisation) timed on
+a bounded row sample.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+L_SITES, PBC, SZ2, LANCZOS_STEPS = 28, True, 0, 200
+METRIC = "lanczos_steps_per_s"
+UNIT = "steps/s"
+DIM = 40116600
+BYTES_PER_ELEM_F32 = 8  # complex FP32
+CPU_REORTH_DEPTH = LANCZOS_STEPS // 2  # mean reorthogonalisation depth of a 200-step run
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-rows", type=int, default=1 << 19)
+    return p.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")
+    return rank, local, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def allreduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([x], dtype=torch.float64)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per SpMV launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "spmv_f32_heisenberg_L28.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out, _ = self.p.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def heis_terms():
+    import models as M
+    return M.heisenberg_terms(L_SITES, PBC)
+
+
+def cpu_baseline(rows, threads):
+    """Reference algorithm on the host cores (oracle port): CSR of `rows`
+    consecutive rows from the middle of the sector, CSR gather SpMV, and the
+    vector algebra of one Lanczos step at the mean full-reorthogonalisation
+    depth; scaled to the whole dimension."""
+    from oracle_ctypes import Oracle, available
+    import models as M
+    if not available("qko"):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "oracle"], check=True)
+    o = Oracle("qko")
+    lib = o.lib
+    c = ctypes
+    lib.qko_sample_create.restype = c.c_void_p
+    terms = heis_terms()
+    cre = np.array([t[0] for t in terms], dtype=np.float64)
+    cim = np.zeros_like(cre)
+    nf = np.array([len(t[1]) for t in terms], dtype=np.int32)
+    fl = [f for t in terms for f in t[1]]
+    ops = (c.c_char_p * len(fl))(*[f[0].encode() for f in fl])
+    sites = np.array([f[1] for f in fl], dtype=np.int32)
+    sec = np.array(M.sector(sz2=SZ2), dtype=np.int32)
+    row0 = DIM // 2 - rows // 2
+    t0 = time.perf_counter()
+    h = lib.qko_sample_create(0, L_SITES, sec.ctypes.data_as(c.POINTER(c.c_int)), len(terms),
+                              cre.ctypes.data_as(c.POINTER(c.c_double)), cim.ctypes.data_as(c.POINTER(c.c_double)),
+                              nf.ctypes.data_as(c.POINTER(c.c_int)), ops, sites.ctypes.data_as(c.POINTER(c.c_int)),
+                              c.c_uint64(row0), c.c_uint64(rows))
+    t_build = time.perf_counter() - t0
+    ta, tv = c.c_double(), c.c_double()
+    lib.qko_sample_time(c.c_void_p(h), 3, CPU_REORTH_DEPTH, threads, c.byref(ta), c.byref(tv))
+    lib.qko_destroy(c.c_void_p(h))
+    per_step = (ta.value + tv.value) * DIM / rows
+    return {"value": 1.0 / per_step, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"rows {row0}..{row0 + rows} of {DIM} (CSR of the sample built in {t_build:.1f}s, untimed); "
+                       f"per step = CSR SpMV {ta.value * 1e3:.2f} ms + reorth-depth-{CPU_REORTH_DEPTH} vector algebra "
+                       f"{tv.value * 1e3:.2f} ms over the sample, scaled by dim/rows")}
+
+
+def run_reference(args, rank, ws):
+    """The reference's CPU algorithm (oracle port; the reference build does not
+    travel), rank 0 only."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(args.cpu_sample_rows, threads)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * LANCZOS_STEPS / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": f"heisenberg_chain_L{L_SITES}_pbc_sz0_{LANCZOS_STEPS}_lanczos_steps", "dim": DIM,
+                       "form": "reference algorithm: host CSR + CSR SpMV + full reorthogonalisation (FP64)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": r["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, local, ws = dist()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+        return
+    import qkrylov_gb300 as qk
+    import models as M
+    from conftest import make_model
+    qk.set_device(local)
+    basis, site, ops = make_model(qk, M.SPIN, L_SITES, M.sector(sz2=SZ2), heis_terms())
+    t0 = time.perf_counter()
+    H = qk.MatrixFreeHamiltonian(basis, site, ops)
+    t_construct = time.perf_counter() - t0
+    assert H.dimension == DIM
+
+    for w in range(args.warmup):
+        qk.lanczos_fixed_steps(H, LANCZOS_STEPS, seed=args.seed + 1000 + w, mixed=True)
+    # ---- timed region: device-resident inputs ---------------------------------
+    res = []
+    qk.synchronize()
+    barrier(ws)
+    l0 = qk.kernel_launches()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            res.append(qk.lanczos_fixed_steps(H, LANCZOS_STEPS, seed=args.seed + k, mixed=True))
+        qk.synchronize()
+        t_total = time.perf_counter() - t0
+    barrier(ws)
+    launches = qk.kernel_launches() - l0
+    t_max = allreduce_max(t_total, ws)
+    value = ws * args.steps * LANCZOS_STEPS / t_max
+    spmv_s = sum(r.seconds_spmv for r in res) / max(1, sum(r.spmv_calls for r in res))
+
+    # ---- e2e: through the C ABI with pinned host buffers -------------------------
+    cudart = _cudart()
+    nbytes = DIM * 16
+    hv0 = _pinned(cudart, nbytes)
+    hev = _pinned(cudart, nbytes)
+    v0 = np.frombuffer((ctypes.c_char * nbytes).from_address(hv0), dtype=np.complex128)
+    ev = np.frombuffer((ctypes.c_char * nbytes).from_address(hev), dtype=np.complex128)
+    rng = np.random.default_rng(args.seed)
+    v0.real[:] = rng.standard_normal(DIM)
+    v0.imag[:] = rng.standard_normal(DIM)
+    qk.lanczos_fixed_steps(H, LANCZOS_STEPS, mixed=True, v0=v0, eigenvector_out=ev)  # warm the host path
+    qk.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    e2e_res = []
+    for k in range(args.steps):
+        e2e_res.append(qk.lanczos_fixed_steps(H, LANCZOS_STEPS, mixed=True, v0=v0, eigenvector_out=ev))
+    qk.synchronize()
+    t_e2e = allreduce_max(time.perf_counter() - t0, ws)
+    e2e_value = ws * args.steps * LANCZOS_STEPS / t_e2e
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c64 (mixed: FP32 vectors/SpMV, FP64-accurate reductions, FP64 refinement)",
+           "data": "synthetic (seeded Philox Gaussian start vectors)",
+           "config": {"workload": f"heisenberg_chain_L{L_SITES}_pbc_sz0_{LANCZOS_STEPS}_lanczos_steps", "dim": DIM,
+                      "lanczos_steps_per_bench_step": LANCZOS_STEPS, "parallelism": f"replicas{ws}",
+                      "l2": "inputs larger than L2 (one FP32 Krylov vector = 321 MB)",
+                      "construct_s": round(t_construct, 3)},
+           "gpu_launches": launches}
+    if rank != 0:
+        return
+    hbm_peak, peak_kind = peaks()
+    alg_bytes = 2 * DIM * BYTES_PER_ELEM_F32
+    achieved = alg_bytes / spmv_s / 1e9
+    tr = profile_traffic()
+    out["roofline"] = {"kernel": "spmv_kernel<uint32,float> (FP32 SpMV)", "bound": "hbm", "achieved": achieved,
+                       "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
+                       "traffic": tr, "algorithmic_bytes_per_launch": alg_bytes,
+                       "launch_ms": spmv_s * 1e3}
+    energies = [r.energy for r in res]
+    out["mixed"] = {"energy": energies[-1], "energy_spread": max(energies) - min(energies),
+                    "residual": res[-1].residual, "selective_steps": res[-1].selective_steps,
+                    "loop_s": res[-1].seconds_loop, "refine_s": res[-1].seconds_refine}
+    out["e2e"] = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes + 64}
+    out["clocks"] = clk.summary()
+    if not args.no_fp64:
+        t0 = time.perf_counter()
+        r64 = qk.lanczos_fixed_steps(H, LANCZOS_STEPS, seed=args.seed, mixed=False)
+        t64 = time.perf_counter() - t0
+        de = abs(res[0].energy - r64.energy)
+        out["fp64"] = {"steps_per_s": LANCZOS_STEPS / t64, "energy": r64.energy, "seconds": t64,
+                       "spmv_ms": 1e3 * r64.seconds_spmv / max(1, r64.spmv_calls),
+                       "form": "reference semantics: FP64 vectors and SpMV, full reorthogonalisation"}
+        out["dE0_vs_fp64"] = {"abs": de, "rel": de / abs(r64.energy), "meets_1e-10": de <= 1e-10 * abs(r64.energy)}
+    if ws == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args.cpu_sample_rows, os.cpu_count() or 1)
+    print(json.dumps(out), flush=True)
+
+
+def _cudart():
+    import glob
+    import ctypes.util
+    names = ["libcudart.so", "libcudart.so.13", ctypes.util.find_library("cudart")]
+    names += glob.glob("/usr/local/cuda/lib64/libcudart.so*") + glob.glob("/usr/local/cuda/targets/*/lib/libcudart.so*")
+    for n in names:
+        if not n:
+            continue
+        try:
+            lib = ctypes.CDLL(n)
+            lib.cudaMallocHost.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
+            return lib
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+def _pinned(cudart, nbytes):
+    p = ctypes.c_void_p()
+    if cudart.cudaMallocHost(ctypes.byref(p), nbytes) != 0:
+        raise RuntimeError("cudaMallocHost failed")
+    return p.value
+
+
+if __name__ == "__main__":
+    main()

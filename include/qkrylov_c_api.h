@@ -1,0 +1,257 @@
+/* qkrylov C ABI, served by libqkrylov_gb300.so (GB300 / sm_103a).
+ *
+ * Part 1 declares every symbol of the reference C API with the reference's
+ * names, argument meaning, float signatures and status codes
+ * (qkrylov: include/qkrylov/c_api.h:14-168, implemented in src/c_api.cpp);
+ * existing callers (the Julia binding's ccall table, bindings/julia/src/*.jl,
+ * or any FFI) relink against this library unchanged.  The float entry points
+ * run the FP64 GPU engine and cast results to float (the reference compiles
+ * its C API into its FP32 engine, CMakeLists.txt:47).
+ *
+ * Part 2 adds what the float ABI cannot carry: FP64 twins (suffix _f64), the
+ * mixed-precision and batched solver forms, device-pointer variants for
+ * callers whose vectors already live on the GPU, an error-string getter and
+ * a debug dump of the generated matrix entries.
+ *
+ * Vectors are complex, interleaved [re, im, re, im, ...], in the reference's
+ * basis order (ascending state integers; Hubbard/t-J states interleaved with
+ * the up electron of site i at bit 2i and the down electron at bit 2i+1).
+ * Every call is synchronous.  A handle is not safe for concurrent use from
+ * several threads; distinct handles are.
+ */
+#ifndef QKRYLOV_GB300_C_API_H
+#define QKRYLOV_GB300_C_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+/* c_api.h:14-16 */
+#define QKRYLOV_SUCCESS                0
+#define QKRYLOV_ERROR_INVALID_ARG     -1
+#define QKRYLOV_ERROR_EXCEPTION       -2
+/* additions: a CUDA runtime error (message in qkrylov_last_error()), and a
+ * bounded device-side wait that gave up */
+#define QKRYLOV_ERROR_CUDA            -3
+#define QKRYLOV_ERROR_DEVICE_TIMEOUT  -4
+
+/* ---------------------------------------------------------------- handles (c_api.h:21-25) */
+typedef struct qkrylov_sector_t*      qkrylov_sector_h;
+typedef struct qkrylov_basis_t*       qkrylov_basis_h;
+typedef struct qkrylov_site_t*        qkrylov_site_h;
+typedef struct qkrylov_opsum_t*       qkrylov_opsum_h;
+typedef struct qkrylov_hamiltonian_t* qkrylov_hamiltonian_h;
+
+/* ================================================================ Part 1: reference ABI */
+
+/* Sector API (c_api.h:30-39) */
+qkrylov_sector_h qkrylov_sector_create(void);
+void             qkrylov_sector_destroy(qkrylov_sector_h sector);
+int              qkrylov_sector_set_sz(qkrylov_sector_h sector, int sz2);
+int              qkrylov_sector_set_hubbard_particles(qkrylov_sector_h sector, int nup, int ndn);
+int              qkrylov_sector_set_n(qkrylov_sector_h sector, int n);
+int              qkrylov_sector_set_nb(qkrylov_sector_h sector, int nb);
+int              qkrylov_sector_get_sz(qkrylov_sector_h sector, int* sz2_out, int* active_out);
+int              qkrylov_sector_get_hubbard_particles(qkrylov_sector_h sector, int* nup_out, int* ndn_out, int* active_out);
+int              qkrylov_sector_get_n(qkrylov_sector_h sector, int* n_out, int* active_out);
+int              qkrylov_sector_get_nb(qkrylov_sector_h sector, int* nb_out, int* active_out);
+
+/* Basis API (c_api.h:44-53).  Bases are built on the host from combinatorial
+ * tables; no GPU is needed until a Hamiltonian is created. */
+qkrylov_basis_h  qkrylov_spinhalf_basis_create(int num_sites, qkrylov_sector_h sector);
+qkrylov_basis_h  qkrylov_fermion_basis_create(int num_sites, qkrylov_sector_h sector);
+qkrylov_basis_h  qkrylov_hubbard_basis_create(int num_sites, qkrylov_sector_h sector);
+qkrylov_basis_h  qkrylov_tj_basis_create(int num_sites, qkrylov_sector_h sector);
+void             qkrylov_basis_destroy(qkrylov_basis_h basis);
+uint64_t         qkrylov_basis_dimension(qkrylov_basis_h basis);
+int              qkrylov_basis_nsites(qkrylov_basis_h basis);
+uint64_t         qkrylov_basis_state(qkrylov_basis_h basis, uint64_t index);
+int64_t          qkrylov_basis_index(qkrylov_basis_h basis, uint64_t state_bitstring);
+int              qkrylov_basis_contains(qkrylov_basis_h basis, uint64_t state_bitstring);
+
+/* Site API (c_api.h:58-62) */
+qkrylov_site_h   qkrylov_spinhalf_site_create(void);
+qkrylov_site_h   qkrylov_fermion_site_create(void);
+qkrylov_site_h   qkrylov_hubbard_site_create(void);
+qkrylov_site_h   qkrylov_tj_site_create(void);
+void             qkrylov_site_destroy(qkrylov_site_h site);
+
+/* OpSum API (c_api.h:67-76) */
+qkrylov_opsum_h  qkrylov_opsum_create(void);
+void             qkrylov_opsum_destroy(qkrylov_opsum_h opsum);
+int              qkrylov_opsum_clear(qkrylov_opsum_h opsum);
+int              qkrylov_opsum_add_term_1body(qkrylov_opsum_h opsum, float coeff_real, float coeff_imag,
+                                             const char* op1, int site1);
+int              qkrylov_opsum_add_term_2body(qkrylov_opsum_h opsum, float coeff_real, float coeff_imag,
+                                             const char* op1, int site1,
+                                             const char* op2, int site2);
+int              qkrylov_opsum_add_term_nbody(qkrylov_opsum_h opsum, float coeff_real, float coeff_imag,
+                                             int n_factors, const char** ops, const int* sites);
+
+/* Matrix-free Hamiltonian API (c_api.h:81-100).  Creation compiles the OpSum
+ * and uploads the basis tables to the current CUDA device; it returns NULL on
+ * failure (unknown operator, site outside the site type's bit range, no GPU). */
+qkrylov_hamiltonian_h qkrylov_hamiltonian_create(qkrylov_basis_h basis,
+                                                qkrylov_site_h site,
+                                                qkrylov_opsum_h opsum);
+void                  qkrylov_hamiltonian_destroy(qkrylov_hamiltonian_h h);
+uint64_t              qkrylov_hamiltonian_dimension(qkrylov_hamiltonian_h h);
+int                   qkrylov_hamiltonian_apply(qkrylov_hamiltonian_h h,
+                                                const float* x_real, const float* x_imag,
+                                                float* y_real, float* y_imag);
+int                   qkrylov_hamiltonian_apply_complex(qkrylov_hamiltonian_h h,
+                                                        const float* x_complex,
+                                                        float* y_complex);
+int                   qkrylov_hamiltonian_diagonal(qkrylov_hamiltonian_h h,
+                                                   float* diag_out);
+
+/* Solvers API (c_api.h:105-168) */
+typedef struct {
+    float energy;
+    int iterations;
+    int converged;
+} qkrylov_lanczos_result_c_t;
+
+typedef struct {
+    int iterations;
+    int converged;
+} qkrylov_davidson_result_c_t;
+
+int qkrylov_lanczos_ground_state(qkrylov_hamiltonian_h h, int maxiter, float tol,
+                                 qkrylov_lanczos_result_c_t* result);
+int qkrylov_lanczos_ground_state_complex(qkrylov_hamiltonian_h h, int maxiter, float tol,
+                                         qkrylov_lanczos_result_c_t* result, float* eigenvector_complex);
+int qkrylov_davidson_lowest_complex(qkrylov_hamiltonian_h h, int n_eig, int max_subspace, float tol,
+                                    float* eigenvalues_out, float* eigenvectors_complex_out,
+                                    qkrylov_davidson_result_c_t* result_info);
+int qkrylov_continued_fraction_coeffs_complex(qkrylov_hamiltonian_h h, const float* phi0_complex, int n_iter,
+                                              float* alphas_out, float* betas_out, float* norm_phi0_out,
+                                              int* num_coeffs_out);
+float qkrylov_evaluate_spectral_function(const float* alphas, const float* betas, size_t n, float norm_phi0,
+                                         float omega, float E0, float eta);
+
+typedef struct {
+    float beta;
+    float partition_function;
+    float internal_energy;
+    float specific_heat;
+} qkrylov_ftlm_result_c_t;
+
+int qkrylov_ftlm(qkrylov_hamiltonian_h h, float beta, int n_random, int n_steps, qkrylov_ftlm_result_c_t* result);
+
+/* ================================================================ Part 2: additions */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* qkrylov_last_error(void);
+
+/* Constrain one spin species alone (the reference's C++ Sector allows it,
+ * sector.hpp:24-31; its C API sets both together). */
+int qkrylov_sector_set_nup(qkrylov_sector_h sector, int nup);
+int qkrylov_sector_set_ndn(qkrylov_sector_h sector, int ndn);
+
+/* OpSum term with double-precision coefficient (c_api.h:75-76 takes float). */
+int qkrylov_opsum_add_term_nbody_f64(qkrylov_opsum_h opsum, double coeff_real, double coeff_imag,
+                                     int n_factors, const char** ops, const int* sites);
+
+/* FP64 twins of the apply / diagonal calls (c_api.h:89-100). */
+int qkrylov_hamiltonian_apply_complex_f64(qkrylov_hamiltonian_h h, const double* x_complex, double* y_complex);
+int qkrylov_hamiltonian_diagonal_f64(qkrylov_hamiltonian_h h, double* diag_out /* real parts, dim */);
+
+/* Same, but x and y are device pointers (reference order) and the work is
+ * queued on `stream` (a cudaStream_t, NULL = legacy default stream); the call
+ * returns without synchronising.  The _f32 form runs the FP32 kernel. */
+int qkrylov_hamiltonian_apply_device_f64(qkrylov_hamiltonian_h h, const void* d_x, void* d_y, void* stream);
+int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* d_x, void* d_y, void* stream);
+
+/* Lanczos ground state, FP64 (reference semantics: full reorthogonalisation,
+ * stop when |E_k - E_{k-1}| < tol; lanczos.cpp:101-202).  The start vector is
+ * the reference's (mt19937(1234), uniform[-1,1] complex) unless v0 (dim complex,
+ * reference order) is given. */
+typedef struct {
+    double energy;           /* reported ground-state energy */
+    double energy_tridiag;   /* lowest eigenvalue of the Lanczos tridiagonal */
+    double residual;         /* ||H psi - E psi|| in FP64, or -1 if not computed */
+    int iterations;
+    int converged;
+    int selective_steps;     /* mixed form: steps re-orthogonalised against the Ritz vector */
+    double seconds_loop;     /* wall time of the Lanczos loop */
+    double seconds_refine;   /* wall time of the FP64 refinement (mixed form) */
+    double seconds_spmv;     /* CUDA-event time of the loop's SpMV launches, summed */
+    int spmv_calls;          /* SpMV launches in the loop */
+} qkrylov_lanczos_result_f64_t;
+
+int qkrylov_lanczos_ground_state_f64(qkrylov_hamiltonian_h h, int maxiter, double tol, const double* v0_complex,
+                                     qkrylov_lanczos_result_f64_t* result, double* eigenvector_complex);
+/* Mixed form: FP32 vectors and FP32 SpMV, compensated (FP64-accurate)
+ * reductions, selective reorthogonalisation against the converged Ritz vector,
+ * then one FP64 SpMV for the Rayleigh quotient and residual.  `energy` is the
+ * refined value. */
+int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, double tol, const double* v0_complex,
+                                       qkrylov_lanczos_result_f64_t* result, double* eigenvector_complex);
+/* Performance form of both: exactly n_steps steps (no early exit); mixed != 0
+ * selects the mixed form.  The start vector is v0_complex (host, reference
+ * order) if given, else a seeded device Gaussian (Philox4x32-10, `seed`).
+ * eigenvector_complex (host, optional) receives the Ritz vector. */
+int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed,
+                                const double* v0_complex, qkrylov_lanczos_result_f64_t* result,
+                                double* eigenvector_complex);
+
+/* Number of kernels this library has launched so far in the process. */
+uint64_t qkrylov_kernel_launches(void);
+
+/* Select the GPU for Hamiltonians created afterwards on this thread (the
+ * reference's Device(id), include/qkrylov/core/device.hpp:27-45), and wait for
+ * all work on the current GPU. */
+int qkrylov_set_device(int device_id);
+int qkrylov_device_synchronize(void);
+
+int qkrylov_davidson_lowest_complex_f64(qkrylov_hamiltonian_h h, int n_eig, int max_subspace, double tol,
+                                        double* eigenvalues_out, double* eigenvectors_complex_out,
+                                        qkrylov_davidson_result_c_t* result_info);
+
+int    qkrylov_continued_fraction_coeffs_complex_f64(qkrylov_hamiltonian_h h, const double* phi0_complex, int n_iter,
+                                                     double* alphas_out, double* betas_out, double* norm_phi0_out,
+                                                     int* num_coeffs_out, int* num_betas_out);
+double qkrylov_evaluate_spectral_function_f64(const double* alphas, const double* betas, size_t n, double norm_phi0,
+                                              double omega, double E0, double eta);
+/* S(omega) on a whole grid: out[k] at omegas[k]. */
+int    qkrylov_evaluate_spectral_grid_f64(const double* alphas, const double* betas, size_t n, double norm_phi0,
+                                          const double* omegas, size_t n_omega, double E0, double eta, double* out);
+
+typedef struct {
+    double beta;
+    double partition_function;
+    double internal_energy;
+    double specific_heat;
+} qkrylov_ftlm_result_f64_t;
+
+int qkrylov_ftlm_f64(qkrylov_hamiltonian_h h, double beta, int n_random, int n_steps, qkrylov_ftlm_result_f64_t* result);
+/* One FTLM run (the reference's random vectors, ftlm.cpp:133-148) evaluated at
+ * n_beta inverse temperatures.  If log_shift is non-NULL the weights use
+ * exp(-beta (E - E_min)) and log_shift[k] = -beta_k E_min, so that
+ * Z_k = partition_function_k * exp(log_shift[k]) stays finite where the
+ * reference's exp(-beta E) overflows. */
+int qkrylov_ftlm_multi_beta_f64(qkrylov_hamiltonian_h h, const double* betas, int n_beta, int n_random, int n_steps,
+                                double* Z_out, double* E_out, double* Cv_out, double* log_shift);
+
+/* Compile statistics of a Hamiltonian: terms per kernel class and diagonal
+ * storage (0: 1-byte code, 1: 2-byte code, 2: full). */
+int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* n_outer, int* n_inner, int* n_mixed, int* n_diag,
+                             int* diag_mode);
+
+/* Every generated matrix entry, rows and columns in the reference's order and
+ * entries of a row in OpSum term order -- the content of the reference's CSR
+ * (matrix_free_hamiltonian.cpp:45-92).  Call once with row_offsets = cols =
+ * vals = NULL to get *nnz_out, then again with arrays of dim+1, nnz and 2*nnz. */
+int qkrylov_hamiltonian_entries(qkrylov_hamiltonian_h h, uint64_t* nnz_out, uint64_t* row_offsets, uint64_t* cols,
+                                double* vals);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QKRYLOV_GB300_C_API_H */

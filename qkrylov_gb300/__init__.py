@@ -1,0 +1,561 @@
+"""qkrylov_gb300: GB300-native matrix-free Hamiltonian apply and Krylov solvers.
+
+The compute library is ``qkrylov_gb300/_lib/libqkrylov_gb300.so`` (CUDA for
+sm_103a behind the C ABI in ``include/qkrylov_c_api.h``).  This module is a thin
+ctypes layer over that ABI that mirrors the reference's Python facade
+(bindings/python/qkrylov/: ``SpinHalfBasis``, ``SpinHalfSite``, ``OpSum``,
+``MatrixFreeHamiltonian(basis, site, ops).apply``, ``lanczos_ground_state``,
+``davidson_lowest``, ``continued_fraction_coeffs``,
+``evaluate_spectral_function``, ``ftlm``) with the same names, argument
+meaning and result objects.  There is no CPU fallback: importing fails if the
+library has not been built (``python -m qkrylov_gb300.build``).
+"""
+import ctypes as _c
+import os as _os
+
+import numpy as _np
+
+_HERE = _os.path.dirname(_os.path.abspath(__file__))
+LIB_PATH = _os.path.join(_HERE, "_lib", "libqkrylov_gb300.so")
+
+SUCCESS, ERROR_INVALID_ARG, ERROR_EXCEPTION, ERROR_CUDA, ERROR_DEVICE_TIMEOUT = 0, -1, -2, -3, -4
+
+_vp, _i, _u64, _i64, _f, _d, _sz = _c.c_void_p, _c.c_int, _c.c_uint64, _c.c_int64, _c.c_float, _c.c_double, _c.c_size_t
+_fp, _dp, _ip, _u64p = _c.POINTER(_c.c_float), _c.POINTER(_c.c_double), _c.POINTER(_c.c_int), _c.POINTER(_c.c_uint64)
+
+
+class LanczosResultC(_c.Structure):
+    _fields_ = [("energy", _f), ("iterations", _i), ("converged", _i)]
+
+
+class DavidsonResultC(_c.Structure):
+    _fields_ = [("iterations", _i), ("converged", _i)]
+
+
+class FTLMResultC(_c.Structure):
+    _fields_ = [("beta", _f), ("partition_function", _f), ("internal_energy", _f), ("specific_heat", _f)]
+
+
+class LanczosResultF64(_c.Structure):
+    _fields_ = [("energy", _d), ("energy_tridiag", _d), ("residual", _d), ("iterations", _i), ("converged", _i),
+                ("selective_steps", _i), ("seconds_loop", _d), ("seconds_refine", _d), ("seconds_spmv", _d),
+                ("spmv_calls", _i)]
+
+
+class FTLMResultF64(_c.Structure):
+    _fields_ = [("beta", _d), ("partition_function", _d), ("internal_energy", _d), ("specific_heat", _d)]
+
+
+# name: (restype, argtypes)
+_SIGS = {
+    "qkrylov_last_error": (_c.c_char_p, []),
+    "qkrylov_sector_create": (_vp, []),
+    "qkrylov_sector_destroy": (None, [_vp]),
+    "qkrylov_sector_set_sz": (_i, [_vp, _i]),
+    "qkrylov_sector_set_hubbard_particles": (_i, [_vp, _i, _i]),
+    "qkrylov_sector_set_n": (_i, [_vp, _i]),
+    "qkrylov_sector_set_nup": (_i, [_vp, _i]),
+    "qkrylov_sector_set_ndn": (_i, [_vp, _i]),
+    "qkrylov_sector_set_nb": (_i, [_vp, _i]),
+    "qkrylov_sector_get_sz": (_i, [_vp, _ip, _ip]),
+    "qkrylov_sector_get_hubbard_particles": (_i, [_vp, _ip, _ip, _ip]),
+    "qkrylov_sector_get_n": (_i, [_vp, _ip, _ip]),
+    "qkrylov_sector_get_nb": (_i, [_vp, _ip, _ip]),
+    "qkrylov_spinhalf_basis_create": (_vp, [_i, _vp]),
+    "qkrylov_fermion_basis_create": (_vp, [_i, _vp]),
+    "qkrylov_hubbard_basis_create": (_vp, [_i, _vp]),
+    "qkrylov_tj_basis_create": (_vp, [_i, _vp]),
+    "qkrylov_basis_destroy": (None, [_vp]),
+    "qkrylov_basis_dimension": (_u64, [_vp]),
+    "qkrylov_basis_nsites": (_i, [_vp]),
+    "qkrylov_basis_state": (_u64, [_vp, _u64]),
+    "qkrylov_basis_index": (_i64, [_vp, _u64]),
+    "qkrylov_basis_contains": (_i, [_vp, _u64]),
+    "qkrylov_spinhalf_site_create": (_vp, []),
+    "qkrylov_fermion_site_create": (_vp, []),
+    "qkrylov_hubbard_site_create": (_vp, []),
+    "qkrylov_tj_site_create": (_vp, []),
+    "qkrylov_site_destroy": (None, [_vp]),
+    "qkrylov_opsum_create": (_vp, []),
+    "qkrylov_opsum_destroy": (None, [_vp]),
+    "qkrylov_opsum_clear": (_i, [_vp]),
+    "qkrylov_opsum_add_term_1body": (_i, [_vp, _f, _f, _c.c_char_p, _i]),
+    "qkrylov_opsum_add_term_2body": (_i, [_vp, _f, _f, _c.c_char_p, _i, _c.c_char_p, _i]),
+    "qkrylov_opsum_add_term_nbody": (_i, [_vp, _f, _f, _i, _c.POINTER(_c.c_char_p), _ip]),
+    "qkrylov_opsum_add_term_nbody_f64": (_i, [_vp, _d, _d, _i, _c.POINTER(_c.c_char_p), _ip]),
+    "qkrylov_hamiltonian_create": (_vp, [_vp, _vp, _vp]),
+    "qkrylov_hamiltonian_destroy": (None, [_vp]),
+    "qkrylov_hamiltonian_dimension": (_u64, [_vp]),
+    "qkrylov_hamiltonian_apply": (_i, [_vp, _fp, _fp, _fp, _fp]),
+    "qkrylov_hamiltonian_apply_complex": (_i, [_vp, _fp, _fp]),
+    "qkrylov_hamiltonian_diagonal": (_i, [_vp, _fp]),
+    "qkrylov_lanczos_ground_state": (_i, [_vp, _i, _f, _c.POINTER(LanczosResultC)]),
+    "qkrylov_lanczos_ground_state_complex": (_i, [_vp, _i, _f, _c.POINTER(LanczosResultC), _fp]),
+    "qkrylov_davidson_lowest_complex": (_i, [_vp, _i, _i, _f, _fp, _fp, _c.POINTER(DavidsonResultC)]),
+    "qkrylov_continued_fraction_coeffs_complex": (_i, [_vp, _fp, _i, _fp, _fp, _fp, _ip]),
+    "qkrylov_evaluate_spectral_function": (_f, [_fp, _fp, _sz, _f, _f, _f, _f]),
+    "qkrylov_ftlm": (_i, [_vp, _f, _i, _i, _c.POINTER(FTLMResultC)]),
+    "qkrylov_hamiltonian_apply_complex_f64": (_i, [_vp, _dp, _dp]),
+    "qkrylov_hamiltonian_diagonal_f64": (_i, [_vp, _dp]),
+    "qkrylov_hamiltonian_apply_device_f64": (_i, [_vp, _vp, _vp, _vp]),
+    "qkrylov_hamiltonian_apply_device_f32": (_i, [_vp, _vp, _vp, _vp]),
+    "qkrylov_lanczos_ground_state_f64": (_i, [_vp, _i, _d, _dp, _c.POINTER(LanczosResultF64), _dp]),
+    "qkrylov_lanczos_ground_state_mixed": (_i, [_vp, _i, _d, _dp, _c.POINTER(LanczosResultF64), _dp]),
+    "qkrylov_lanczos_fixed_steps": (_i, [_vp, _i, _u64, _i, _dp, _c.POINTER(LanczosResultF64), _dp]),
+    "qkrylov_kernel_launches": (_u64, []),
+    "qkrylov_set_device": (_i, [_i]),
+    "qkrylov_device_synchronize": (_i, []),
+    "qkrylov_davidson_lowest_complex_f64": (_i, [_vp, _i, _i, _d, _dp, _dp, _c.POINTER(DavidsonResultC)]),
+    "qkrylov_continued_fraction_coeffs_complex_f64": (_i, [_vp, _dp, _i, _dp, _dp, _dp, _ip, _ip]),
+    "qkrylov_evaluate_spectral_function_f64": (_d, [_dp, _dp, _sz, _d, _d, _d, _d]),
+    "qkrylov_evaluate_spectral_grid_f64": (_i, [_dp, _dp, _sz, _d, _dp, _sz, _d, _d, _dp]),
+    "qkrylov_ftlm_f64": (_i, [_vp, _d, _i, _i, _c.POINTER(FTLMResultF64)]),
+    "qkrylov_ftlm_multi_beta_f64": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, _dp, _dp]),
+    "qkrylov_hamiltonian_info": (_i, [_vp, _ip, _ip, _ip, _ip, _ip]),
+    "qkrylov_hamiltonian_entries": (_i, [_vp, _u64p, _u64p, _u64p, _dp]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded C-ABI library (ctypes.CDLL) with argument types declared."""
+    global _lib
+    if _lib is None:
+        if not _os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m qkrylov_gb300.build`")
+        L = _c.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class QKrylovError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"qkrylov error {code}: {msg}")
+        self.code = code
+
+
+def _check(rc):
+    if rc != SUCCESS:
+        raise QKrylovError(rc, (lib().qkrylov_last_error() or b"").decode())
+    return rc
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_fp)
+
+
+def _cvec(x, n, dtype=_np.complex128):
+    x = _np.ascontiguousarray(x, dtype=dtype)
+    if x.ndim != 1 or x.shape[0] != n:
+        raise ValueError(f"vector of length {n} expected, got shape {x.shape}")
+    return x
+
+
+# ------------------------------------------------------------------ model objects
+class _Handle:
+    _destroy = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            getattr(_lib, self._destroy)(h)
+            self._h = None
+
+
+class Sector(_Handle):
+    """Quantum-number sector (include/qkrylov/symmetry/sector.hpp:10-41)."""
+    _destroy = "qkrylov_sector_destroy"
+
+    def __init__(self, sz2=None, nup=None, ndn=None, n=None, nb=None):
+        self._h = lib().qkrylov_sector_create()
+        if sz2 is not None:
+            _check(lib().qkrylov_sector_set_sz(self._h, int(sz2)))
+        if nup is not None and ndn is not None:
+            _check(lib().qkrylov_sector_set_hubbard_particles(self._h, int(nup), int(ndn)))
+        elif nup is not None:
+            _check(lib().qkrylov_sector_set_nup(self._h, int(nup)))
+        elif ndn is not None:
+            _check(lib().qkrylov_sector_set_ndn(self._h, int(ndn)))
+        if n is not None:
+            _check(lib().qkrylov_sector_set_n(self._h, int(n)))
+        if nb is not None:
+            _check(lib().qkrylov_sector_set_nb(self._h, int(nb)))
+
+
+class Basis(_Handle):
+    _destroy = "qkrylov_basis_destroy"
+    _create = None
+
+    def __init__(self, N, sector=None):
+        self._sector = sector
+        self._h = getattr(lib(), self._create)(int(N), sector._h if sector else None)
+        if not self._h:
+            raise ValueError((lib().qkrylov_last_error() or b"").decode())
+
+    @property
+    def size(self):
+        return int(lib().qkrylov_basis_dimension(self._h))
+
+    @property
+    def nsites(self):
+        return int(lib().qkrylov_basis_nsites(self._h))
+
+    def state(self, i):
+        return int(lib().qkrylov_basis_state(self._h, int(i)))
+
+    def index(self, s):
+        return int(lib().qkrylov_basis_index(self._h, int(s)))
+
+    def contains(self, s):
+        return bool(lib().qkrylov_basis_contains(self._h, int(s)))
+
+    def states(self):
+        return _np.array([self.state(i) for i in range(self.size)], dtype=_np.uint64)
+
+
+class SpinHalfBasis(Basis):
+    """Spin-1/2 chain; ``sz`` is the total Sz (the sector stores 2*Sz)."""
+    _create = "qkrylov_spinhalf_basis_create"
+
+    def __init__(self, N, conserve_sz=False, sz=None):
+        if sz is not None or conserve_sz:
+            super().__init__(N, Sector(sz2=int(round(2 * (sz or 0)))))
+        else:
+            super().__init__(N)
+
+
+class FermionBasis(Basis):
+    _create = "qkrylov_fermion_basis_create"
+
+    def __init__(self, N, conserve_n=False, n=None):
+        if n is not None or conserve_n:
+            super().__init__(N, Sector(n=int(n or 0)))
+        else:
+            super().__init__(N)
+
+
+class HubbardBasis(Basis):
+    _create = "qkrylov_hubbard_basis_create"
+
+    def __init__(self, N, nup=None, ndn=None):
+        super().__init__(N, Sector(nup=nup, ndn=ndn) if (nup is not None or ndn is not None) else None)
+
+
+class TJBasis(HubbardBasis):
+    _create = "qkrylov_tj_basis_create"
+
+
+class Site(_Handle):
+    _destroy = "qkrylov_site_destroy"
+    _create = None
+
+    def __init__(self):
+        self._h = getattr(lib(), self._create)()
+
+
+class SpinHalfSite(Site):
+    _create = "qkrylov_spinhalf_site_create"
+
+
+class FermionSite(Site):
+    _create = "qkrylov_fermion_site_create"
+
+
+class HubbardSite(Site):
+    _create = "qkrylov_hubbard_site_create"
+
+
+class TJSite(Site):
+    _create = "qkrylov_tj_site_create"
+
+
+class OpSum(_Handle):
+    """Ordered list of ``coeff * op(site) * op(site) ...`` terms
+    (include/qkrylov/operators/opsum.hpp:13-48)."""
+    _destroy = "qkrylov_opsum_destroy"
+
+    def __init__(self):
+        self._h = lib().qkrylov_opsum_create()
+        self.terms = []
+
+    def add_term(self, coeff, *ops_sites):
+        """add_term(coeff, "Sz", 0, "Sz", 1, ...)"""
+        if len(ops_sites) < 2 or len(ops_sites) % 2:
+            raise ValueError("expected coeff followed by (op, site) pairs")
+        ops = [str(o) for o in ops_sites[0::2]]
+        sites = [int(s) for s in ops_sites[1::2]]
+        c = complex(coeff)
+        arr = (_c.c_char_p * len(ops))(*[o.encode() for o in ops])
+        sarr = (_c.c_int * len(sites))(*sites)
+        _check(lib().qkrylov_opsum_add_term_nbody_f64(self._h, c.real, c.imag, len(ops), arr, sarr))
+        self.terms.append((c, list(zip(ops, sites))))
+        return self
+
+    def __iadd__(self, term):
+        if isinstance(term, tuple):
+            return self.add_term(*term)
+        raise TypeError("OpSum += (coeff, op, site, ...)")
+
+    def __len__(self):
+        return len(self.terms)
+
+
+class MatrixFreeHamiltonian(_Handle):
+    """y = H x on the GPU (include/qkrylov/hamiltonian/matrix_free_hamiltonian.hpp:24-77)."""
+    _destroy = "qkrylov_hamiltonian_destroy"
+
+    def __init__(self, basis, site, ops):
+        self.basis, self.site, self.ops = basis, site, ops
+        self._h = lib().qkrylov_hamiltonian_create(basis._h, site._h, ops._h)
+        if not self._h:
+            raise ValueError((lib().qkrylov_last_error() or b"").decode() or "hamiltonian creation failed")
+
+    @property
+    def dimension(self):
+        return int(lib().qkrylov_hamiltonian_dimension(self._h))
+
+    def apply(self, x):
+        x = _cvec(x, self.dimension)
+        y = _np.empty_like(x)
+        _check(lib().qkrylov_hamiltonian_apply_complex_f64(self._h, _dptr(x.view(_np.float64)), _dptr(y.view(_np.float64))))
+        return y
+
+    __matmul__ = apply
+
+    def apply_device(self, x_ptr, y_ptr, stream=None, fp32=False):
+        """Device pointers (reference order); queued on `stream`, not synchronised."""
+        fn = lib().qkrylov_hamiltonian_apply_device_f32 if fp32 else lib().qkrylov_hamiltonian_apply_device_f64
+        _check(fn(self._h, _c.c_void_p(x_ptr), _c.c_void_p(y_ptr), _c.c_void_p(stream or 0)))
+
+    def diagonal(self):
+        d = _np.empty(self.dimension, dtype=_np.float64)
+        _check(lib().qkrylov_hamiltonian_diagonal_f64(self._h, _dptr(d)))
+        return d
+
+    def info(self):
+        v = [_c.c_int() for _ in range(5)]
+        _check(lib().qkrylov_hamiltonian_info(self._h, *[_c.byref(x) for x in v]))
+        return dict(zip(["n_outer", "n_inner", "n_mixed", "n_diag", "diag_mode"], [x.value for x in v]))
+
+    def entries(self):
+        """(row_offsets, cols, vals) of every generated entry, reference order."""
+        nnz = _c.c_uint64()
+        _check(lib().qkrylov_hamiltonian_entries(self._h, _c.byref(nnz), None, None, None))
+        n = self.dimension
+        ro = _np.zeros(n + 1, dtype=_np.uint64)
+        cols = _np.zeros(max(1, nnz.value), dtype=_np.uint64)
+        vals = _np.zeros(2 * max(1, nnz.value), dtype=_np.float64)
+        _check(lib().qkrylov_hamiltonian_entries(self._h, _c.byref(nnz), ro.ctypes.data_as(_u64p),
+                                                 cols.ctypes.data_as(_u64p), _dptr(vals)))
+        return ro, cols[: nnz.value], vals[: 2 * nnz.value].view(_np.complex128)
+
+    def to_sparse(self):
+        import scipy.sparse as sp
+        ro, cols, vals = self.entries()
+        n = self.dimension
+        return sp.csr_matrix((vals, cols.astype(_np.int64), ro.astype(_np.int64)), shape=(n, n))
+
+    def aslinearoperator(self):
+        import scipy.sparse.linalg as sla
+        n = self.dimension
+        return sla.LinearOperator(shape=(n, n), matvec=self.apply, dtype=_np.complex128)
+
+    def __repr__(self):
+        return f"MatrixFreeHamiltonian(dim={self.dimension})"
+
+
+# ------------------------------------------------------------------ solvers
+class LanczosResult:
+    def __init__(self, energy, eigenvector=None, iterations=0, converged=False, residual=None, energy_tridiag=None,
+                 raw=None):
+        self.energy, self.eigenvector = energy, eigenvector
+        self.iterations, self.converged = iterations, converged
+        self.residual, self.energy_tridiag, self.raw = residual, energy_tridiag, raw
+
+    def __repr__(self):
+        return f"LanczosResult(energy={self.energy:.10f})"
+
+
+def lanczos_ground_state(H, maxiter=200, tol=1e-12, v0=None, mixed=False, return_state=True):
+    """Ground state by Lanczos.  ``mixed=False`` is the reference algorithm in
+    FP64 (src/solvers/lanczos.cpp:101-202); ``mixed=True`` is the FP32-vector
+    form with FP64 refinement."""
+    n = H.dimension
+    r = LanczosResultF64()
+    ev = _np.empty(n, dtype=_np.complex128) if return_state else None
+    v0p = _dptr(_cvec(v0, n).view(_np.float64)) if v0 is not None else None
+    fn = lib().qkrylov_lanczos_ground_state_mixed if mixed else lib().qkrylov_lanczos_ground_state_f64
+    _check(fn(H._h, int(maxiter), float(tol), v0p, _c.byref(r), _dptr(ev.view(_np.float64)) if return_state else None))
+    return LanczosResult(r.energy, ev, r.iterations, bool(r.converged), r.residual if r.residual >= 0 else None,
+                         r.energy_tridiag, r)
+
+
+def lanczos_fixed_steps(H, n_steps, seed=0, mixed=True, v0=None, eigenvector_out=None):
+    """Exactly n_steps Lanczos steps (performance form).  v0 / eigenvector_out
+    are optional host arrays (complex128, reference order)."""
+    r = LanczosResultF64()
+    n = H.dimension
+    v0p = _dptr(_cvec(v0, n).view(_np.float64)) if v0 is not None else None
+    evp = _dptr(eigenvector_out.view(_np.float64)) if eigenvector_out is not None else None
+    _check(lib().qkrylov_lanczos_fixed_steps(H._h, int(n_steps), int(seed), int(bool(mixed)), v0p, _c.byref(r), evp))
+    return r
+
+
+def kernel_launches():
+    return int(lib().qkrylov_kernel_launches())
+
+
+def set_device(device_id):
+    _check(lib().qkrylov_set_device(int(device_id)))
+
+
+def synchronize():
+    _check(lib().qkrylov_device_synchronize())
+
+
+class DavidsonResult:
+    def __init__(self, eigenvalues, eigenvectors, iterations=0, converged=False):
+        self.eigenvalues, self.eigenvectors = eigenvalues, eigenvectors
+        self.iterations, self.converged = iterations, converged
+
+    def __repr__(self):
+        return f"DavidsonResult(energies={self.eigenvalues})"
+
+
+def davidson_lowest(H, n_eig=1, max_subspace=20, tol=1e-8, return_vectors=True):
+    n = H.dimension
+    k = min(int(n_eig), n)
+    ev = _np.zeros(max(1, int(n_eig)))
+    vecs = _np.zeros((max(1, k), n), dtype=_np.complex128) if return_vectors else None
+    info = DavidsonResultC()
+    _check(lib().qkrylov_davidson_lowest_complex_f64(H._h, int(n_eig), int(max_subspace), float(tol), _dptr(ev),
+                                                     _dptr(vecs.view(_np.float64)) if return_vectors else None,
+                                                     _c.byref(info)))
+    return DavidsonResult(ev[:k], list(vecs[:k]) if return_vectors else None, info.iterations, bool(info.converged))
+
+
+class DynamicsResult:
+    def __init__(self, alphas, betas, norm_phi0):
+        self.alphas, self.betas, self.norm_phi0 = alphas, betas, norm_phi0
+
+
+def continued_fraction_coeffs(H, phi0, n_iter=100):
+    n = H.dimension
+    p = _cvec(phi0, n)
+    a = _np.zeros(n_iter)
+    b = _np.zeros(n_iter)
+    nrm = _c.c_double()
+    na = _c.c_int()
+    nb = _c.c_int()
+    _check(lib().qkrylov_continued_fraction_coeffs_complex_f64(H._h, _dptr(p.view(_np.float64)), int(n_iter), _dptr(a),
+                                                               _dptr(b), _c.byref(nrm), _c.byref(na), _c.byref(nb)))
+    return DynamicsResult(a[: na.value], b[: nb.value], nrm.value)
+
+
+def evaluate_spectral_function(res, omega, E0, eta=0.1):
+    a = _np.ascontiguousarray(res.alphas, dtype=_np.float64)
+    b = _np.ascontiguousarray(res.betas, dtype=_np.float64)
+    if b.size < max(1, a.size):
+        b = _np.concatenate([b, _np.zeros(max(1, a.size) - b.size)])
+    om = _np.atleast_1d(_np.asarray(omega, dtype=_np.float64))
+    out = _np.zeros_like(om)
+    _check(lib().qkrylov_evaluate_spectral_grid_f64(_dptr(a), _dptr(b), a.size, float(res.norm_phi0), _dptr(om), om.size,
+                                                    float(E0), float(eta), _dptr(out)))
+    return float(out[0]) if _np.ndim(omega) == 0 else out
+
+
+class FTLMResult:
+    def __init__(self, beta, partition_function, internal_energy, specific_heat, log_shift=None):
+        self.beta, self.partition_function = beta, partition_function
+        self.internal_energy, self.specific_heat, self.log_shift = internal_energy, specific_heat, log_shift
+
+
+def ftlm(H, beta, n_random=50, n_steps=100, shifted=False):
+    """FTLM with the reference's random vectors (src/solvers/ftlm.cpp:123-170).
+    ``beta`` may be a scalar or an array (one run, many temperatures)."""
+    b = _np.atleast_1d(_np.asarray(beta, dtype=_np.float64))
+    Z, E, C = _np.zeros_like(b), _np.zeros_like(b), _np.zeros_like(b)
+    ls = _np.zeros_like(b) if shifted else None
+    _check(lib().qkrylov_ftlm_multi_beta_f64(H._h, _dptr(b), b.size, int(n_random), int(n_steps), _dptr(Z), _dptr(E),
+                                             _dptr(C), _dptr(ls) if shifted else None))
+    if _np.ndim(beta) == 0:
+        return FTLMResult(float(b[0]), float(Z[0]), float(E[0]), float(C[0]), float(ls[0]) if shifted else None)
+    return FTLMResult(b, Z, E, C, ls)
+
+
+# ------------------------------------------------------------------ expression sugar
+class LocalOp:
+    def __init__(self, name, site):
+        self.name, self.site = name, site
+
+    def __mul__(self, other):
+        if isinstance(other, LocalOp):
+            return Term(1.0, [self, other])
+        if isinstance(other, (int, float, complex)):
+            return Term(complex(other), [self])
+        return NotImplemented
+
+    def __rmul__(self, other):
+        if isinstance(other, (int, float, complex)):
+            return Term(complex(other), [self])
+        return NotImplemented
+
+
+class Term:
+    def __init__(self, coeff, ops):
+        self.coeff, self.ops = coeff, ops
+
+    def __mul__(self, other):
+        if isinstance(other, LocalOp):
+            return Term(self.coeff, self.ops + [other])
+        if isinstance(other, Term):
+            return Term(self.coeff * other.coeff, self.ops + other.ops)
+        if isinstance(other, (int, float, complex)):
+            return Term(self.coeff * complex(other), self.ops)
+        return NotImplemented
+
+    __rmul__ = __mul__
+
+    def __add__(self, other):
+        return Expr([self]) + other
+
+
+class Expr:
+    def __init__(self, terms):
+        self.terms = list(terms)
+
+    def __add__(self, other):
+        if isinstance(other, Term):
+            return Expr(self.terms + [other])
+        if isinstance(other, Expr):
+            return Expr(self.terms + other.terms)
+        return NotImplemented
+
+
+def _opsum_iadd(self, x):
+    if isinstance(x, Term):
+        x = Expr([x])
+    if isinstance(x, Expr):
+        for t in x.terms:
+            args = []
+            for o in t.ops:
+                args += [o.name, o.site]
+            self.add_term(t.coeff, *args)
+        return self
+    return _tuple_iadd(self, x)
+
+
+_tuple_iadd = OpSum.__iadd__
+OpSum.__iadd__ = _opsum_iadd
+
+for _name in ("Sz", "Sp", "Sm", "Sx", "Sy", "CdagUp", "CUp", "CdagDn", "CDn", "Nup", "Ndn", "Nupdn", "N", "C", "Cdag", "Id"):
+    globals()[_name] = (lambda nm: (lambda i: LocalOp(nm, i)))(_name)

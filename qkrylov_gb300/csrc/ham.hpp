@@ -1,0 +1,141 @@
+// Hamiltonian object, device vectors and the Krylov-algebra launchers.
+#pragma once
+
+#include "qkg.hpp"
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <memory>
+#include <vector>
+
+namespace qkg {
+
+// Owning device buffer.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    explicit DBuf(size_t n) { alloc(n); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DBuf& operator=(DBuf&& o) noexcept { reset(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; return *this; }
+    ~DBuf() { reset(); }
+    void alloc(size_t n);
+    void reset();
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
+
+// Per-precision copy of the compiled term lists.
+struct TermSet {
+    DBuf outer, inner, mixed, diag, all, vars;
+    int n_outer = 0, n_inner = 0, n_mixed = 0, n_diag = 0, n_all = 0;
+};
+
+class Hamiltonian {
+public:
+    Hamiltonian(std::shared_ptr<Basis> basis, SiteKind site, const std::vector<Term>& terms);
+    ~Hamiltonian();
+
+    uint64_t dim() const { return basis_->dim; }
+    Basis& basis() { return *basis_; }
+    cudaStream_t stream() const { return stream_; }
+    int device() const { return dev_; }
+    const DevBasis& dbasis() const { return *db_; }
+    bool permuted() const { return basis_->permuted; }
+    bool all_real() const { return all_real_; }
+
+    // y = H x on device vectors in internal order (interleaved complex).
+    void apply_f64(const double2* x, double2* y, cudaStream_t s) const;
+    void apply_f32(const float2* x, float2* y, cudaStream_t s) const;
+
+    // Diagonal H_ii (complex, internal order) into a device buffer.
+    void diagonal_f64(double2* d, cudaStream_t s) const;
+
+    // Reference order <-> internal order for device vectors.
+    void to_internal_f64(const double2* ref, double2* in, cudaStream_t s) const;
+    void to_reference_f64(const double2* in, double2* ref, cudaStream_t s) const;
+    void to_internal_f32(const float2* ref, float2* in, cudaStream_t s) const;
+    void to_reference_f32(const float2* in, float2* ref, cudaStream_t s) const;
+
+    // Debug: every generated matrix entry, rows in internal order, entries in
+    // OpSum term order (row_offsets[dim+1], cols = internal indices, vals).
+    void emit_entries(std::vector<uint64_t>& row_offsets, std::vector<uint64_t>& cols,
+                      std::vector<std::complex<double>>& vals) const;
+
+    // Host-side helpers
+    std::vector<std::complex<double>> diagonal_host_ref() const;  // reference order
+
+    // Compile statistics
+    int n_outer() const { return t64_.n_outer; }
+    int n_inner() const { return t64_.n_inner; }
+    int n_mixed() const { return t64_.n_mixed; }
+    int n_diag() const { return t64_.n_diag; }
+    int diag_mode() const { return diag_mode_; }
+    size_t n_items() const { return n_items_; }
+
+private:
+    void build_diagonal();
+    template <class S> void upload_terms(const std::vector<HostTerm>& ht);
+
+    std::shared_ptr<Basis> basis_;
+    const DevBasis* db_ = nullptr;
+    SiteKind site_;
+    int dev_ = 0;
+    cudaStream_t stream_ = nullptr;
+    bool wide_ = false;       // states need 64 bits
+    bool all_real_ = true;
+    std::vector<HostTerm> hterms_;
+    TermSet t64_, t32_;
+    DBuf items_;
+    size_t n_items_ = 0;
+    int diag_mode_ = DIAG_U8;
+    DBuf dcode_, dtab64_, dtab32_, dfull64_, dfull32_;
+    int n_dtab_ = 0;
+};
+
+// ------------------------------------------------------------ Krylov algebra
+// Reductions return to the host (one sync); FP32 reductions are compensated
+// (Ogita-Rump-Oishi Dot2: TwoProduct via fma, TwoSum accumulation) so their
+// error is that of a computation in twice the working precision.
+struct Workspace {
+    DBuf partial;     // per-block partial sums
+    DBuf result;      // device-side result slots
+    double* host = nullptr;  // pinned host result slots
+    size_t cap_partials = 0;
+    explicit Workspace(size_t max_blocks_times_k = 1 << 16);
+    ~Workspace();
+};
+
+std::complex<double> dot_f64(const double2* x, const double2* y, uint64_t n, Workspace& ws, cudaStream_t s);
+std::complex<double> dot_f32(const float2* x, const float2* y, uint64_t n, Workspace& ws, cudaStream_t s);
+double nrm2sq_f64(const double2* x, uint64_t n, Workspace& ws, cudaStream_t s);
+double nrm2sq_f32(const float2* x, uint64_t n, Workspace& ws, cudaStream_t s);
+void axpy_f64(std::complex<double> a, const double2* x, double2* y, uint64_t n, cudaStream_t s);
+void axpy_f32(std::complex<double> a, const float2* x, float2* y, uint64_t n, cudaStream_t s);
+void scal_f64(double a, double2* x, uint64_t n, cudaStream_t s);
+void scal_f32(double a, float2* x, uint64_t n, cudaStream_t s);
+void f64_to_f32(const double2* x, float2* y, uint64_t n, cudaStream_t s);
+void f32_to_f64(const float2* x, double2* y, uint64_t n, cudaStream_t s);
+// w -= alpha v + beta vprev (vprev may be null); returns ||w||^2 (fused pass).
+double lanczos_update_f64(double2* w, const double2* v, const double2* vprev, double alpha, double beta, uint64_t n,
+                          Workspace& ws, cudaStream_t s);
+double lanczos_update_f32(float2* w, const float2* v, const float2* vprev, double alpha, double beta, uint64_t n,
+                          Workspace& ws, cudaStream_t s);
+// out[j] = <V_j, w> for j < k (one pass over w, V given as device pointer array).
+void mdot_f64(const double2* const* V_dev, int k, const double2* w, uint64_t n, std::complex<double>* out,
+              Workspace& ws, cudaStream_t s);
+void mdot_f32(const float2* const* V_dev, int k, const float2* w, uint64_t n, std::complex<double>* out,
+              Workspace& ws, cudaStream_t s);
+// w += sum_j c[j] V_j  (c given on the host, k <= 1024)
+void mcombine_f64(const double2* const* V_dev, int k, const std::complex<double>* c, double2* w, uint64_t n,
+                  Workspace& ws, cudaStream_t s);
+void mcombine_f32(const float2* const* V_dev, int k, const std::complex<double>* c, float2* w, uint64_t n,
+                  Workspace& ws, cudaStream_t s);
+// Davidson preconditioner t_i = r_i / (d_i - lambda) with the reference's clamp.
+void davidson_precond_f64(const double2* r, const double2* d, double lambda, double2* t, uint64_t n, cudaStream_t s);
+
+}  // namespace qkg

@@ -1,0 +1,700 @@
+// Matrix-free y = Hx on the GPU.
+//
+// The reference builds a host CSR once (src/hamiltonian/matrix_free_hamiltonian.cpp:45-92)
+// and applies it with one thread per row (:156-167), which costs 20 bytes of
+// matrix stream per nonzero and int32 offsets that overflow beyond 2^31
+// nonzeros.  Here nothing but the diagonal (as a 1- or 2-byte code per row) is
+// stored: every off-diagonal entry is regenerated in the kernel from the
+// compiled term masks (compile.cpp) and ranked with the basis tables
+// (basis.cpp).  The row sum is
+//     y[a] = d[a] x[a] + sum_t conj(amp_t(s_a)) x[rank(s_a ^ X_t)]
+// which is the reference's y[alpha] = sum_j vals[j] x[cols[j]] with the
+// diagonal entries of one row pre-summed in term order (the reference's own
+// diagonal accumulation, :86-89).
+//
+// Work decomposition: rows are grouped into work items that lie inside one
+// outer block (constant high bits a).  Terms are classified at construction:
+//   outer  - flips and conditions only on outer bits: validity and the target
+//            block are the same for every row of the item, so one warp
+//            evaluates them once per item and each row only adds x[row+delta]
+//            (a coalesced, contiguous stream from the neighbouring block);
+//   inner  - flips and conditions only on inner bits: the target lies in the
+//            same block, rank = block offset + inner_rank[b'];
+//   mixed  - everything else: full rank of the target.
+#include "ham.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <set>
+#include <utility>
+
+namespace qkg {
+
+void DBuf::alloc(size_t n) {
+    reset();
+    if (n) {
+        QKG_CUDA(cudaMalloc(&p, n));
+        bytes = n;
+    }
+}
+void DBuf::reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kChunk = 1024;
+constexpr int kMaxOuter = 256;
+constexpr size_t kSmemTermBudget = 40 * 1024;
+
+template <class S, class A>
+struct alignas(16) KTerm {
+    S C, V, X, J;
+    A ar, ai;
+    uint32_t flags, var0;
+};
+template <class A>
+struct alignas(16) KVar {
+    uint64_t sm, pf;
+    A a0r, a0i, a1r, a1i;
+};
+
+template <class T> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+
+template <class S> __device__ __forceinline__ int popcnt(S x);
+template <> __device__ __forceinline__ int popcnt<uint32_t>(uint32_t x) { return __popc(x); }
+template <> __device__ __forceinline__ int popcnt<uint64_t>(uint64_t x) { return __popcll(x); }
+
+template <class S>
+__device__ __forceinline__ bool in_basis(const DevBasis& b, S s) {
+    if (b.ngroups > 0 && popcnt<S>(s & (S)b.gmask[0]) != b.gpop[0]) return false;
+    if (b.ngroups > 1 && popcnt<S>(s & (S)b.gmask[1]) != b.gpop[1]) return false;
+    if (b.no_double && (s & (s >> b.N) & (S)((1ULL << b.N) - 1))) return false;
+    return true;
+}
+
+__device__ __forceinline__ uint64_t outer_off(const DevBasis& b, uint64_t a) {
+    return b.idx32 ? (uint64_t)__ldg(static_cast<const uint32_t*>(b.outer_off) + a)
+                   : (uint64_t)__ldg(static_cast<const unsigned long long*>(b.outer_off) + a);
+}
+
+template <class S>
+__device__ __forceinline__ uint64_t rank_table(const DevBasis& b, S s) {
+    const uint64_t a = (uint64_t)(s >> b.n_in);
+    const S bb = s & (S)b.in_mask;
+    return outer_off(b, a) + (b.inner_all ? (uint64_t)bb : (uint64_t)__ldg(b.inner_rank + bb));
+}
+
+template <class S>
+__device__ __forceinline__ uint64_t rank_search(const DevBasis& b, S s) {
+    const uint64_t a = b.n_out ? (uint64_t)((uint64_t)s >> b.n_in) : 0;
+    uint64_t lo = outer_off(b, a), hi = outer_off(b, a + 1);
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (__ldg(reinterpret_cast<const unsigned long long*>(b.states_int) + mid) < (uint64_t)s) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <class S, int RANK>
+__device__ __forceinline__ uint64_t rank_of(const DevBasis& b, S s) {
+    return RANK == RANK_TABLE ? rank_table<S>(b, s) : rank_search<S>(b, s);
+}
+
+// Row state of row r of a work item.
+template <class S, int RANK>
+__device__ __forceinline__ S row_state(const DevBasis& b, const WorkItem& it, uint32_t r) {
+    if (RANK == RANK_TABLE) {
+        const S bb = b.inner_all ? (S)(it.inner_base + r) : (S)__ldg(b.inner_state + it.inner_base + r);
+        return (S)(((uint64_t)it.a << b.n_in) | (uint64_t)bb);
+    }
+    return (S)__ldg(reinterpret_cast<const unsigned long long*>(b.states_int) + it.row0 + r);
+}
+
+template <class S, class A>
+__device__ __forceinline__ void term_amp(const KTerm<S, A>& t, S s, const KVar<A>* __restrict__ vars, A& ar, A& ai) {
+    ar = t.ar;
+    ai = t.ai;
+    const uint32_t nv = (t.flags >> 8) & 0xffu;
+    for (uint32_t k = 0; k < nv; ++k) {
+        const KVar<A> v = vars[t.var0 + k];
+        const bool sel = (((uint64_t)s ^ v.pf) & v.sm) == v.sm;
+        const A cr = sel ? v.a1r : v.a0r, ci = sel ? v.a1i : v.a0i;
+        const A nr = ar * cr - ai * ci;
+        ai = ar * ci + ai * cr;
+        ar = nr;
+    }
+    if (popcnt<S>(s & t.J) & 1) {
+        ar = -ar;
+        ai = -ai;
+    }
+}
+
+template <class A, class X2>
+__device__ __forceinline__ void cmac(A& r, A& i, A ar, A ai, const X2& x, bool real) {
+    r = fma(ar, (A)x.x, r);
+    i = fma(ar, (A)x.y, i);
+    if (!real) {
+        r = fma(-ai, (A)x.y, r);
+        i = fma(ai, (A)x.x, i);
+    }
+}
+
+template <class S, class A>
+struct SpmvParams {
+    DevBasis b;
+    const WorkItem* items;
+    const KTerm<S, A>* outer;
+    const KTerm<S, A>* inner;
+    const KTerm<S, A>* mixed;
+    const KVar<A>* vars;
+    int n_outer, n_inner, n_mixed, n_vars;
+    int terms_in_smem;
+    int real;
+    int diag_mode;
+    const void* dcode;
+    const void* dtab;   // A pairs
+    const void* dfull;  // T pairs per row (DIAG_FULL)
+};
+
+template <class S, class T, class A, int RANK>
+__global__ void __launch_bounds__(kBlock) spmv_kernel(const SpmvParams<S, A> p, const typename V2<T>::t* __restrict__ x,
+                                                      typename V2<T>::t* __restrict__ y) {
+    using T2 = typename V2<T>::t;
+    using Term = KTerm<S, A>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_nvalid;
+    __shared__ int s_ti[kMaxOuter];
+    __shared__ long long s_delta[kMaxOuter];
+
+    const Term* outer = p.outer;
+    const Term* inner = p.inner;
+    const Term* mixed = p.mixed;
+    const KVar<A>* vars = p.vars;
+    if (p.terms_in_smem) {
+        // Stage the term lists (read by every row) in shared memory.
+        Term* st = reinterpret_cast<Term*>(smem_raw);
+        const int nt = p.n_outer + p.n_inner + p.n_mixed;
+        for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+            st[i] = i < p.n_outer ? p.outer[i] : (i < p.n_outer + p.n_inner ? p.inner[i - p.n_outer] : p.mixed[i - p.n_outer - p.n_inner]);
+        }
+        KVar<A>* sv = reinterpret_cast<KVar<A>*>(st + nt);
+        for (int i = threadIdx.x; i < p.n_vars; i += blockDim.x) sv[i] = p.vars[i];
+        outer = st;
+        inner = st + p.n_outer;
+        mixed = st + p.n_outer + p.n_inner;
+        vars = sv;
+        __syncthreads();
+    }
+    const DevBasis& b = p.b;
+    const bool real = p.real;
+
+    const WorkItem it = p.items[blockIdx.x];
+    uint64_t block_off = 0;
+    int nvalid = 0;
+    if (RANK == RANK_TABLE) {
+        block_off = outer_off(b, it.a);
+        if (p.n_outer > 0) {
+            if (threadIdx.x < 32) {
+                // One warp finds the outer terms valid for this block, in term order.
+                const S s0 = row_state<S, RANK>(b, it, 0);
+                int base = 0;
+                for (int t0 = 0; t0 < p.n_outer; t0 += 32) {
+                    const int ti = t0 + (int)threadIdx.x;
+                    bool ok = false;
+                    long long delta = 0;
+                    if (ti < p.n_outer) {
+                        const Term t = outer[ti];
+                        if ((s0 & t.C) == t.V) {
+                            const S s2 = s0 ^ t.X;
+                            if (!(t.flags & 1u) || in_basis<S>(b, s2)) {
+                                ok = true;
+                                delta = (long long)outer_off(b, (uint64_t)(s2 >> b.n_in)) - (long long)block_off;
+                            }
+                        }
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, ok);
+                    if (ok) {
+                        const int pos = base + __popc(m & ((1u << threadIdx.x) - 1u));
+                        s_ti[pos] = ti;
+                        s_delta[pos] = delta;
+                    }
+                    base += __popc(m);
+                }
+                if (threadIdx.x == 0) s_nvalid = base;
+            }
+            __syncthreads();
+            nvalid = s_nvalid;
+        }
+    }
+
+    for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
+        const uint64_t row = it.row0 + r;
+        const S s = row_state<S, RANK>(b, it, r);
+        A accr, acci;
+        {
+            A dr, di;
+            if (p.diag_mode == DIAG_U8) {
+                const uint32_t c = __ldg(static_cast<const uint8_t*>(p.dcode) + row);
+                const A* tab = static_cast<const A*>(p.dtab);
+                dr = tab[2 * c];
+                di = tab[2 * c + 1];
+            } else if (p.diag_mode == DIAG_U16) {
+                const uint32_t c = __ldg(static_cast<const uint16_t*>(p.dcode) + row);
+                const A* tab = static_cast<const A*>(p.dtab);
+                dr = tab[2 * c];
+                di = tab[2 * c + 1];
+            } else {
+                const T2 d = static_cast<const T2*>(p.dfull)[row];
+                dr = (A)d.x;
+                di = (A)d.y;
+            }
+            const T2 xv = x[row];
+            accr = dr * (A)xv.x;
+            acci = dr * (A)xv.y;
+            if (!real) {
+                accr = fma(-di, (A)xv.y, accr);
+                acci = fma(di, (A)xv.x, acci);
+            }
+        }
+        for (int k = 0; k < nvalid; ++k) {
+            const Term t = outer[s_ti[k]];
+            A ar, ai;
+            term_amp<S, A>(t, s, vars, ar, ai);
+            const T2 xv = x[row + s_delta[k]];
+            cmac<A>(accr, acci, ar, ai, xv, real);
+        }
+        for (int k = 0; k < p.n_inner; ++k) {
+            const Term t = inner[k];
+            if ((s & t.C) != t.V) continue;
+            const S s2 = s ^ t.X;
+            if ((t.flags & 1u) && !in_basis<S>(b, s2)) continue;
+            const S b2 = s2 & (S)b.in_mask;
+            const uint64_t idx = block_off + (b.inner_all ? (uint64_t)b2 : (uint64_t)__ldg(b.inner_rank + b2));
+            A ar, ai;
+            term_amp<S, A>(t, s, vars, ar, ai);
+            const T2 xv = x[idx];
+            cmac<A>(accr, acci, ar, ai, xv, real);
+        }
+        for (int k = 0; k < p.n_mixed; ++k) {
+            const Term t = mixed[k];
+            if ((s & t.C) != t.V) continue;
+            const S s2 = s ^ t.X;
+            if ((t.flags & 1u) && !in_basis<S>(b, s2)) continue;
+            const uint64_t idx = rank_of<S, RANK>(b, s2);
+            A ar, ai;
+            term_amp<S, A>(t, s, vars, ar, ai);
+            const T2 xv = x[idx];
+            cmac<A>(accr, acci, ar, ai, xv, real);
+        }
+        T2 out;
+        out.x = (T)accr;
+        out.y = (T)acci;
+        y[row] = out;
+    }
+}
+
+// Diagonal of H, summed in OpSum term order like the reference
+// (matrix_free_hamiltonian.cpp:86-89).
+template <class S, int RANK>
+__global__ void __launch_bounds__(kBlock) diag_kernel(const DevBasis b, const WorkItem* __restrict__ items,
+                                                      const KTerm<S, double>* __restrict__ diag, int n_diag,
+                                                      const KVar<double>* __restrict__ vars, double2* __restrict__ out) {
+    const WorkItem it = items[blockIdx.x];
+    for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
+        const S s = row_state<S, RANK>(b, it, r);
+        double sr = 0.0, si = 0.0;
+        for (int k = 0; k < n_diag; ++k) {
+            const KTerm<S, double> t = diag[k];
+            if ((s & t.C) != t.V) continue;
+            double ar, ai;
+            term_amp<S, double>(t, s, vars, ar, ai);
+            sr += ar;
+            si += ai;
+        }
+        out[it.row0 + r] = make_double2(sr, si);
+    }
+}
+
+// Code each diagonal value by binary search in a sorted table of bit patterns;
+// values not in the table are collected (bounded) for the next round.
+__global__ void diag_code_kernel(const double2* __restrict__ d, uint64_t n, const ulonglong2* __restrict__ tab, int ntab,
+                                 void* codes, int code_bytes, ulonglong2* missing, unsigned long long* n_missing,
+                                 unsigned long long cap) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 v = d[i];
+        const unsigned long long kx = (unsigned long long)__double_as_longlong(v.x);
+        const unsigned long long ky = (unsigned long long)__double_as_longlong(v.y);
+        int lo = 0, hi = ntab;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            const ulonglong2 t = tab[mid];
+            if (t.x < kx || (t.x == kx && t.y < ky)) lo = mid + 1;
+            else hi = mid;
+        }
+        int code = 0;
+        if (lo < ntab && tab[lo].x == kx && tab[lo].y == ky) {
+            code = lo;
+        } else {
+            const unsigned long long slot = atomicAdd(n_missing, 1ULL);
+            if (slot < cap) missing[slot] = make_ulonglong2(kx, ky);
+        }
+        if (code_bytes == 1) static_cast<uint8_t*>(codes)[i] = (uint8_t)code;
+        else static_cast<uint16_t*>(codes)[i] = (uint16_t)code;
+    }
+}
+
+template <class A>
+__global__ void diag_expand_kernel(const void* codes, int code_bytes, const A* tab, uint64_t n, typename V2<A>::t* out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = code_bytes == 1 ? static_cast<const uint8_t*>(codes)[i] : static_cast<const uint16_t*>(codes)[i];
+        typename V2<A>::t o;
+        o.x = tab[2 * c];
+        o.y = tab[2 * c + 1];
+        out[i] = o;
+    }
+}
+
+__global__ void d2f_kernel(const double2* __restrict__ a, float2* __restrict__ b, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+template <class V, class I>
+__global__ void gather_kernel(const V* __restrict__ src, V* __restrict__ dst, const I* __restrict__ perm, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+template <class V, class I>
+__global__ void scatter_kernel(const V* __restrict__ src, V* __restrict__ dst, const I* __restrict__ perm, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[perm[i]] = src[i];
+}
+
+// Debug emitter: every entry of every row in term order (count pass, then fill).
+template <class S, int RANK>
+__global__ void emit_kernel(const DevBasis b, const WorkItem* __restrict__ items, const KTerm<S, double>* __restrict__ all,
+                            int n_all, const KVar<double>* __restrict__ vars, const unsigned long long* __restrict__ offs,
+                            unsigned long long* __restrict__ counts, unsigned long long* __restrict__ cols,
+                            double2* __restrict__ vals) {
+    const WorkItem it = items[blockIdx.x];
+    for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
+        const uint64_t row = it.row0 + r;
+        const S s = row_state<S, RANK>(b, it, r);
+        unsigned long long k = 0;
+        for (int q = 0; q < n_all; ++q) {
+            const KTerm<S, double> t = all[q];
+            if ((s & t.C) != t.V) continue;
+            const S s2 = s ^ t.X;
+            if ((t.flags & 1u) && !in_basis<S>(b, s2)) continue;
+            if (offs) {
+                double ar, ai;
+                term_amp<S, double>(t, s, vars, ar, ai);
+                cols[offs[row] + k] = rank_of<S, RANK>(b, s2);
+                vals[offs[row] + k] = make_double2(ar, ai);
+            }
+            ++k;
+        }
+        if (!offs) counts[row] = k;
+    }
+}
+
+inline int grid_for(uint64_t n) {
+    uint64_t g = (n + kBlock - 1) / kBlock;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, 152ull * 32));
+}
+
+template <class S, class A>
+KTerm<S, A> to_kterm(const HostTerm& h, uint32_t var0) {
+    KTerm<S, A> k;
+    k.C = (S)h.C; k.V = (S)h.V; k.X = (S)h.X; k.J = (S)h.J;
+    k.ar = (A)h.amp.real(); k.ai = (A)h.amp.imag();
+    k.flags = (h.check ? 1u : 0u) | ((uint32_t)h.vars.size() << 8);
+    k.var0 = var0;
+    return k;
+}
+
+template <class T>
+void upload_vec(DBuf& buf, const std::vector<T>& v) {
+    buf.alloc(std::max<size_t>(1, v.size()) * sizeof(T));
+    if (!v.empty()) QKG_CUDA(cudaMemcpy(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------ host
+template <class S>
+void Hamiltonian::upload_terms(const std::vector<HostTerm>& ht) {
+    // Classification (see top of file).
+    std::vector<const HostTerm*> outer, inner, mixed, diag;
+    const uint64_t inm = basis_->rank_kind == RANK_TABLE ? db_->in_mask : 0;
+    for (const auto& h : ht) {
+        if (h.X == 0) { diag.push_back(&h); continue; }
+        if (basis_->rank_kind == RANK_TABLE && ((h.X | h.C) & inm) == 0) outer.push_back(&h);
+        else if (basis_->rank_kind == RANK_TABLE && ((h.X | h.C) & ~inm) == 0) inner.push_back(&h);
+        else mixed.push_back(&h);
+    }
+    if ((int)outer.size() > kMaxOuter) {
+        mixed.insert(mixed.end(), outer.begin(), outer.end());
+        outer.clear();
+    }
+    auto build = [&](auto tag, TermSet& ts) {
+        using A = decltype(tag);
+        std::vector<KVar<A>> vars;
+        auto conv = [&](const std::vector<const HostTerm*>& lst) {
+            std::vector<KTerm<S, A>> out;
+            for (const HostTerm* h : lst) {
+                out.push_back(to_kterm<S, A>(*h, (uint32_t)vars.size()));
+                for (const DVar& v : h->vars)
+                    vars.push_back({v.sm, v.pf, (A)v.a0r, (A)v.a0i, (A)v.a1r, (A)v.a1i});
+            }
+            return out;
+        };
+        std::vector<const HostTerm*> allp;
+        for (const auto& h : ht) allp.push_back(&h);
+        auto ko = conv(outer), ki = conv(inner), km = conv(mixed), kd = conv(diag), ka = conv(allp);
+        upload_vec(ts.outer, ko); upload_vec(ts.inner, ki); upload_vec(ts.mixed, km);
+        upload_vec(ts.diag, kd); upload_vec(ts.all, ka); upload_vec(ts.vars, vars);
+        ts.n_outer = (int)ko.size(); ts.n_inner = (int)ki.size(); ts.n_mixed = (int)km.size();
+        ts.n_diag = (int)kd.size(); ts.n_all = (int)ka.size();
+    };
+    build(double(), t64_);
+    build(float(), t32_);
+}
+
+Hamiltonian::Hamiltonian(std::shared_ptr<Basis> basis, SiteKind site, const std::vector<Term>& terms)
+    : basis_(std::move(basis)), site_(site) {
+    QKG_CUDA(cudaGetDevice(&dev_));
+    hterms_ = compile_terms(*basis_, site, terms);
+    db_ = &basis_->device(dev_);
+    wide_ = basis_->nbits > 32;
+    for (const auto& h : hterms_) {
+        if (h.amp.imag() != 0.0) all_real_ = false;
+        for (const auto& v : h.vars) if (v.a0i != 0.0 || v.a1i != 0.0) all_real_ = false;
+    }
+    if (wide_) upload_terms<uint64_t>(hterms_);
+    else upload_terms<uint32_t>(hterms_);
+    auto items = basis_->work_items(kChunk);
+    n_items_ = items.size();
+    upload_vec(items_, items);
+    QKG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    build_diagonal();
+}
+
+Hamiltonian::~Hamiltonian() {
+    if (stream_) {
+        cudaStreamSynchronize(stream_);
+        cudaStreamDestroy(stream_);
+    }
+}
+
+void Hamiltonian::build_diagonal() {
+    const uint64_t n = dim();
+    dfull64_.alloc(std::max<uint64_t>(1, n) * sizeof(double2));
+    if (n) {
+        const DevBasis b = *db_;
+        if (wide_) {
+            auto f = b.rank_kind == RANK_TABLE ? diag_kernel<uint64_t, RANK_TABLE> : diag_kernel<uint64_t, RANK_SEARCH>;
+            f<<<(unsigned)n_items_, kBlock, 0, stream_>>>(b, items_.as<WorkItem>(), t64_.diag.as<KTerm<uint64_t, double>>(),
+                                                         t64_.n_diag, t64_.vars.as<KVar<double>>(), dfull64_.as<double2>());
+        } else {
+            auto f = b.rank_kind == RANK_TABLE ? diag_kernel<uint32_t, RANK_TABLE> : diag_kernel<uint32_t, RANK_SEARCH>;
+            f<<<(unsigned)n_items_, kBlock, 0, stream_>>>(b, items_.as<WorkItem>(), t64_.diag.as<KTerm<uint32_t, double>>(),
+                                                         t64_.n_diag, t64_.vars.as<KVar<double>>(), dfull64_.as<double2>());
+        }
+        QKG_LAUNCHED();
+    }
+    // Distinct diagonal values -> small table + per-row code.
+    std::set<std::pair<uint64_t, uint64_t>> table;
+    const unsigned long long cap = 1 << 20;
+    DBuf missing(cap * sizeof(ulonglong2)), nmiss(sizeof(unsigned long long)), tabbuf;
+    DBuf codes(std::max<uint64_t>(1, n) * 2);
+    std::vector<ulonglong2> hmiss;
+    bool full = false;
+    for (int round = 0; round < 64 && n; ++round) {
+        std::vector<ulonglong2> tv;
+        for (const auto& kv : table) tv.push_back(make_ulonglong2(kv.first, kv.second));
+        upload_vec(tabbuf, tv);
+        const int code_bytes = table.size() <= 256 ? 1 : 2;
+        QKG_CUDA(cudaMemsetAsync(nmiss.p, 0, sizeof(unsigned long long), stream_));
+        diag_code_kernel<<<grid_for(n), kBlock, 0, stream_>>>(dfull64_.as<double2>(), n, tabbuf.as<ulonglong2>(),
+                                                              (int)tv.size(), codes.p, code_bytes,
+                                                              missing.as<ulonglong2>(), nmiss.as<unsigned long long>(), cap);
+        QKG_LAUNCHED();
+        unsigned long long nm = 0;
+        QKG_CUDA(cudaMemcpyAsync(&nm, nmiss.p, sizeof(nm), cudaMemcpyDeviceToHost, stream_));
+        QKG_CUDA(cudaStreamSynchronize(stream_));
+        if (nm == 0) {
+            diag_mode_ = code_bytes == 1 ? DIAG_U8 : DIAG_U16;
+            break;
+        }
+        const size_t take = (size_t)std::min<unsigned long long>(nm, cap);
+        hmiss.resize(take);
+        QKG_CUDA(cudaMemcpy(hmiss.data(), missing.p, take * sizeof(ulonglong2), cudaMemcpyDeviceToHost));
+        for (const auto& m : hmiss) table.insert({m.x, m.y});
+        if (table.size() > 65536) { full = true; break; }
+    }
+    if (!n) { diag_mode_ = DIAG_U8; table.insert({0, 0}); }
+    if (full) {
+        diag_mode_ = DIAG_FULL;
+        dfull32_.alloc(n * sizeof(float2));
+        d2f_kernel<<<grid_for(n), kBlock, 0, stream_>>>(dfull64_.as<double2>(), dfull32_.as<float2>(), n);
+        QKG_LAUNCHED();
+    } else {
+        std::vector<double> t64;
+        std::vector<float> t32;
+        for (const auto& kv : table) {
+            double re, im;
+            std::memcpy(&re, &kv.first, 8);
+            std::memcpy(&im, &kv.second, 8);
+            t64.push_back(re); t64.push_back(im);
+            t32.push_back((float)re); t32.push_back((float)im);
+        }
+        n_dtab_ = (int)table.size();
+        upload_vec(dtab64_, t64);
+        upload_vec(dtab32_, t32);
+        const size_t cb = diag_mode_ == DIAG_U8 ? 1 : 2;
+        dcode_.alloc(std::max<uint64_t>(1, n) * cb);
+        // The last round wrote every code with the final table's width.
+        if (n) QKG_CUDA(cudaMemcpyAsync(dcode_.p, codes.p, n * cb, cudaMemcpyDeviceToDevice, stream_));
+        QKG_CUDA(cudaStreamSynchronize(stream_));
+        dfull64_.reset();
+    }
+    QKG_CUDA(cudaStreamSynchronize(stream_));
+}
+
+template <class S, class T, class A>
+static void launch_spmv(const DevBasis& b, const TermSet& ts, const DBuf& items, size_t n_items, bool real, int diag_mode,
+                        const DBuf& dcode, const DBuf& dtab, const DBuf& dfull, const typename V2<T>::t* x,
+                        typename V2<T>::t* y, cudaStream_t s) {
+    if (!n_items) return;
+    SpmvParams<S, A> p;
+    p.b = b;
+    p.items = items.as<WorkItem>();
+    p.outer = ts.outer.as<KTerm<S, A>>();
+    p.inner = ts.inner.as<KTerm<S, A>>();
+    p.mixed = ts.mixed.as<KTerm<S, A>>();
+    p.vars = ts.vars.as<KVar<A>>();
+    p.n_outer = ts.n_outer; p.n_inner = ts.n_inner; p.n_mixed = ts.n_mixed;
+    p.n_vars = (int)(ts.vars.bytes / sizeof(KVar<A>));
+    const size_t smem = (size_t)(p.n_outer + p.n_inner + p.n_mixed) * sizeof(KTerm<S, A>) + (size_t)p.n_vars * sizeof(KVar<A>);
+    p.terms_in_smem = smem <= kSmemTermBudget;
+    p.real = real;
+    p.diag_mode = diag_mode;
+    p.dcode = dcode.p;
+    p.dtab = dtab.p;
+    p.dfull = dfull.p;
+    const size_t dyn = p.terms_in_smem ? smem : 0;
+    if (b.rank_kind == RANK_TABLE)
+        spmv_kernel<S, T, A, RANK_TABLE><<<(unsigned)n_items, kBlock, dyn, s>>>(p, x, y);
+    else
+        spmv_kernel<S, T, A, RANK_SEARCH><<<(unsigned)n_items, kBlock, dyn, s>>>(p, x, y);
+    QKG_LAUNCHED();
+}
+
+void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const {
+    const DBuf& full = dfull64_;
+    if (wide_)
+        launch_spmv<uint64_t, double, double>(*db_, t64_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab64_, full, x, y, s);
+    else
+        launch_spmv<uint32_t, double, double>(*db_, t64_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab64_, full, x, y, s);
+}
+
+void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
+    if (wide_)
+        launch_spmv<uint64_t, float, float>(*db_, t32_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab32_, dfull32_, x, y, s);
+    else
+        launch_spmv<uint32_t, float, float>(*db_, t32_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab32_, dfull32_, x, y, s);
+}
+
+void Hamiltonian::diagonal_f64(double2* d, cudaStream_t s) const {
+    const uint64_t n = dim();
+    if (!n) return;
+    if (diag_mode_ == DIAG_FULL) {
+        QKG_CUDA(cudaMemcpyAsync(d, dfull64_.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        return;
+    }
+    diag_expand_kernel<double><<<grid_for(n), kBlock, 0, s>>>(dcode_.p, diag_mode_ == DIAG_U8 ? 1 : 2, dtab64_.as<double>(), n, d);
+    QKG_LAUNCHED();
+}
+
+std::vector<std::complex<double>> Hamiltonian::diagonal_host_ref() const {
+    const uint64_t n = dim();
+    std::vector<std::complex<double>> out(n);
+    if (!n) return out;
+    DBuf a(n * sizeof(double2)), b2(n * sizeof(double2));
+    diagonal_f64(a.as<double2>(), stream_);
+    to_reference_f64(a.as<double2>(), b2.as<double2>(), stream_);
+    QKG_CUDA(cudaMemcpyAsync(out.data(), b2.p, n * sizeof(double2), cudaMemcpyDeviceToHost, stream_));
+    QKG_CUDA(cudaStreamSynchronize(stream_));
+    return out;
+}
+
+template <class V>
+static void permute(const DevBasis& b, bool permuted, const V* src, V* dst, uint64_t n, bool to_int, cudaStream_t s) {
+    if (!n) return;
+    if (!permuted) {
+        if (src != dst) QKG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(V), cudaMemcpyDeviceToDevice, s));
+        return;
+    }
+    if (b.idx32) {
+        const uint32_t* perm = static_cast<const uint32_t*>(b.ref_of_int);
+        if (to_int) gather_kernel<V, uint32_t><<<grid_for(n), kBlock, 0, s>>>(src, dst, perm, n);
+        else scatter_kernel<V, uint32_t><<<grid_for(n), kBlock, 0, s>>>(src, dst, perm, n);
+    } else {
+        const uint64_t* perm = static_cast<const uint64_t*>(b.ref_of_int);
+        if (to_int) gather_kernel<V, uint64_t><<<grid_for(n), kBlock, 0, s>>>(src, dst, perm, n);
+        else scatter_kernel<V, uint64_t><<<grid_for(n), kBlock, 0, s>>>(src, dst, perm, n);
+    }
+    QKG_LAUNCHED();
+}
+
+void Hamiltonian::to_internal_f64(const double2* r, double2* i, cudaStream_t s) const { permute(*db_, permuted(), r, i, dim(), true, s); }
+void Hamiltonian::to_reference_f64(const double2* i, double2* r, cudaStream_t s) const { permute(*db_, permuted(), i, r, dim(), false, s); }
+void Hamiltonian::to_internal_f32(const float2* r, float2* i, cudaStream_t s) const { permute(*db_, permuted(), r, i, dim(), true, s); }
+void Hamiltonian::to_reference_f32(const float2* i, float2* r, cudaStream_t s) const { permute(*db_, permuted(), i, r, dim(), false, s); }
+
+void Hamiltonian::emit_entries(std::vector<uint64_t>& row_offsets, std::vector<uint64_t>& cols,
+                               std::vector<std::complex<double>>& vals) const {
+    const uint64_t n = dim();
+    row_offsets.assign(n + 1, 0);
+    cols.clear();
+    vals.clear();
+    if (!n) return;
+    DBuf counts(n * 8), offs((n + 1) * 8);
+    const DevBasis b = *db_;
+    auto run = [&](const unsigned long long* o, unsigned long long* c, unsigned long long* cl, double2* v) {
+        if (wide_) {
+            auto f = b.rank_kind == RANK_TABLE ? emit_kernel<uint64_t, RANK_TABLE> : emit_kernel<uint64_t, RANK_SEARCH>;
+            f<<<(unsigned)n_items_, kBlock, 0, stream_>>>(b, items_.as<WorkItem>(), t64_.all.as<KTerm<uint64_t, double>>(),
+                                                         t64_.n_all, t64_.vars.as<KVar<double>>(), o, c, cl, v);
+        } else {
+            auto f = b.rank_kind == RANK_TABLE ? emit_kernel<uint32_t, RANK_TABLE> : emit_kernel<uint32_t, RANK_SEARCH>;
+            f<<<(unsigned)n_items_, kBlock, 0, stream_>>>(b, items_.as<WorkItem>(), t64_.all.as<KTerm<uint32_t, double>>(),
+                                                         t64_.n_all, t64_.vars.as<KVar<double>>(), o, c, cl, v);
+        }
+        QKG_LAUNCHED();
+    };
+    run(nullptr, counts.as<unsigned long long>(), nullptr, nullptr);
+    std::vector<uint64_t> cnt(n);
+    QKG_CUDA(cudaMemcpyAsync(cnt.data(), counts.p, n * 8, cudaMemcpyDeviceToHost, stream_));
+    QKG_CUDA(cudaStreamSynchronize(stream_));
+    for (uint64_t i = 0; i < n; ++i) row_offsets[i + 1] = row_offsets[i] + cnt[i];
+    const uint64_t nnz = row_offsets[n];
+    QKG_CUDA(cudaMemcpy(offs.p, row_offsets.data(), (n + 1) * 8, cudaMemcpyHostToDevice));
+    DBuf dc(std::max<uint64_t>(1, nnz) * 8), dv(std::max<uint64_t>(1, nnz) * sizeof(double2));
+    run(offs.as<unsigned long long>(), nullptr, dc.as<unsigned long long>(), dv.as<double2>());
+    cols.resize(nnz);
+    vals.resize(nnz);
+    QKG_CUDA(cudaMemcpyAsync(cols.data(), dc.p, nnz * 8, cudaMemcpyDeviceToHost, stream_));
+    QKG_CUDA(cudaMemcpyAsync(vals.data(), dv.p, nnz * sizeof(double2), cudaMemcpyDeviceToHost, stream_));
+    QKG_CUDA(cudaStreamSynchronize(stream_));
+}
+
+}  // namespace qkg

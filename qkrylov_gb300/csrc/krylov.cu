@@ -1,0 +1,474 @@
+// Krylov vector algebra on device-resident complex vectors.
+//
+// The reference runs every BLAS-1 call as its own Kokkos kernel and returns
+// each reduction to the host (include/qkrylov/linalg/vector_ops.hpp:14-137);
+// its full reorthogonalisation is k sequential dot+axpy pairs
+// (src/solvers/lanczos.cpp:148-151).  Here the Lanczos three-term update and
+// the norm are one fused pass, the projections against k stored vectors are
+// one pass over w (classical Gram-Schmidt), and reductions finish on the
+// device with one host read.
+//
+// FP32 reductions use error-free transformations (Ogita, Rump & Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2):
+// each product a*b is split exactly into p + e with one fma, p is added with
+// Knuth's TwoSum and the rounding errors are carried in a second float, so a
+// thread's partial sum is as accurate as if computed in twice the working
+// precision.  Partials are then combined in FP64.  This keeps the reductions
+// off GB300's low-rate FP64 pipe.
+#include "ham.hpp"
+
+#include <algorithm>
+
+namespace qkg {
+
+namespace {
+constexpr int kThreads = 256;
+
+inline int stream_grid(uint64_t n) {
+    const uint64_t g = (n + kThreads - 1) / kThreads;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, 152ull * 8));
+}
+
+// ---- compensated FP32 accumulation ----------------------------------------
+struct FF {  // unevaluated sum hi + lo
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add_prod(FF& acc, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);  // exact: a*b = p + e
+    const float t = acc.hi + p;      // TwoSum(acc.hi, p)
+    const float z = t - acc.hi;
+    const float err = (acc.hi - (t - z)) + (p - z);
+    acc.hi = t;
+    acc.lo += err + e;
+}
+__device__ __forceinline__ double ff_value(const FF& a) { return (double)a.hi + (double)a.lo; }
+
+// ---- block reduction of double pairs ---------------------------------------
+__device__ __forceinline__ double2 warp_sum(double2 v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+__device__ __forceinline__ double2 block_sum(double2 v) {
+    __shared__ double2 sh[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : make_double2(0.0, 0.0);
+    if (wid == 0) v = warp_sum(v);
+    return v;
+}
+
+// dot: sum conj(x_i) y_i
+__global__ void dot64_kernel(const double2* __restrict__ x, const double2* __restrict__ y, uint64_t n, double2* part) {
+    double re = 0.0, im = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 a = x[i], b = y[i];
+        re = fma(a.x, b.x, re);
+        re = fma(a.y, b.y, re);
+        im = fma(a.x, b.y, im);
+        im = fma(-a.y, b.x, im);
+    }
+    const double2 s = block_sum(make_double2(re, im));
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void dot32_kernel(const float2* __restrict__ x, const float2* __restrict__ y, uint64_t n, double2* part) {
+    FF re{0.f, 0.f}, im{0.f, 0.f};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 a = x[i], b = y[i];
+        ff_add_prod(re, a.x, b.x);
+        ff_add_prod(re, a.y, b.y);
+        ff_add_prod(im, a.x, b.y);
+        ff_add_prod(im, -a.y, b.x);
+    }
+    const double2 s = block_sum(make_double2(ff_value(re), ff_value(im)));
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void nrm64_kernel(const double2* __restrict__ x, uint64_t n, double2* part) {
+    double acc = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 a = x[i];
+        acc = fma(a.x, a.x, acc);
+        acc = fma(a.y, a.y, acc);
+    }
+    const double2 s = block_sum(make_double2(acc, 0.0));
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void nrm32_kernel(const float2* __restrict__ x, uint64_t n, double2* part) {
+    FF acc{0.f, 0.f};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 a = x[i];
+        ff_add_prod(acc, a.x, a.x);
+        ff_add_prod(acc, a.y, a.y);
+    }
+    const double2 s = block_sum(make_double2(ff_value(acc), 0.0));
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// Sum `nparts` partials for each of `k` columns (column j at part[j*stride ...]).
+__global__ void finish_kernel(const double2* __restrict__ part, int nparts, int stride, double2* out) {
+    const int j = blockIdx.x;
+    double re = 0.0, im = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        const double2 v = part[(size_t)j * stride + i];
+        re += v.x;
+        im += v.y;
+    }
+    const double2 s = block_sum(make_double2(re, im));
+    if (threadIdx.x == 0) out[j] = s;
+}
+
+__global__ void axpy64_kernel(double ar, double ai, const double2* __restrict__ x, double2* __restrict__ y, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 a = x[i];
+        double2 b = y[i];
+        b.x = fma(ar, a.x, fma(-ai, a.y, b.x));
+        b.y = fma(ar, a.y, fma(ai, a.x, b.y));
+        y[i] = b;
+    }
+}
+__global__ void axpy32_kernel(float ar, float ai, const float2* __restrict__ x, float2* __restrict__ y, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 a = x[i];
+        float2 b = y[i];
+        b.x = fmaf(ar, a.x, fmaf(-ai, a.y, b.x));
+        b.y = fmaf(ar, a.y, fmaf(ai, a.x, b.y));
+        y[i] = b;
+    }
+}
+__global__ void scal64_kernel(double a, double2* __restrict__ x, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        double2 v = x[i];
+        v.x *= a;
+        v.y *= a;
+        x[i] = v;
+    }
+}
+__global__ void scal32_kernel(float a, float2* __restrict__ x, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float2 v = x[i];
+        v.x *= a;
+        v.y *= a;
+        x[i] = v;
+    }
+}
+__global__ void d2f_kernel2(const double2* __restrict__ a, float2* __restrict__ b, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void f2d_kernel(const float2* __restrict__ a, double2* __restrict__ b, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        b[i] = make_double2((double)a[i].x, (double)a[i].y);
+}
+
+// w <- w - alpha v - beta vprev, and ||w||^2 of the result (one pass).
+__global__ void lupd64_kernel(double2* __restrict__ w, const double2* __restrict__ v, const double2* __restrict__ vp,
+                              double alpha, double beta, uint64_t n, double2* part) {
+    double acc = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        double2 a = w[i];
+        const double2 b = v[i];
+        a.x = fma(-alpha, b.x, a.x);
+        a.y = fma(-alpha, b.y, a.y);
+        if (vp) {
+            const double2 c = vp[i];
+            a.x = fma(-beta, c.x, a.x);
+            a.y = fma(-beta, c.y, a.y);
+        }
+        w[i] = a;
+        acc = fma(a.x, a.x, acc);
+        acc = fma(a.y, a.y, acc);
+    }
+    const double2 s = block_sum(make_double2(acc, 0.0));
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void lupd32_kernel(float2* __restrict__ w, const float2* __restrict__ v, const float2* __restrict__ vp,
+                              float alpha, float beta, uint64_t n, double2* part) {
+    FF acc{0.f, 0.f};
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float2 a = w[i];
+        const float2 b = v[i];
+        a.x = fmaf(-alpha, b.x, a.x);
+        a.y = fmaf(-alpha, b.y, a.y);
+        if (vp) {
+            const float2 c = vp[i];
+            a.x = fmaf(-beta, c.x, a.x);
+            a.y = fmaf(-beta, c.y, a.y);
+        }
+        w[i] = a;
+        ff_add_prod(acc, a.x, a.x);
+        ff_add_prod(acc, a.y, a.y);
+    }
+    const double2 s = block_sum(make_double2(ff_value(acc), 0.0));
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// Projections <V_j, w> for a group of up to KB vectors per block column.
+constexpr int KB = 8;
+template <class T2, bool F32>
+__global__ void mdot_kernel(const T2* const* __restrict__ V, int k, const T2* __restrict__ w, uint64_t n, double2* part,
+                            int stride) {
+    const int j0 = blockIdx.y * KB;
+    const int kk = min(KB, k - j0);
+    double re[KB], im[KB];
+    FF fre[KB], fim[KB];
+#pragma unroll
+    for (int q = 0; q < KB; ++q) { re[q] = im[q] = 0.0; fre[q] = fim[q] = FF{0.f, 0.f}; }
+    const T2* vp[KB];
+#pragma unroll
+    for (int q = 0; q < KB; ++q) vp[q] = (q < kk) ? V[j0 + q] : nullptr;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const T2 b = w[i];
+#pragma unroll
+        for (int q = 0; q < KB; ++q) {
+            if (q < kk) {
+                const T2 a = vp[q][i];
+                if (F32) {
+                    ff_add_prod(fre[q], (float)a.x, (float)b.x);
+                    ff_add_prod(fre[q], (float)a.y, (float)b.y);
+                    ff_add_prod(fim[q], (float)a.x, (float)b.y);
+                    ff_add_prod(fim[q], -(float)a.y, (float)b.x);
+                } else {
+                    re[q] = fma((double)a.x, (double)b.x, re[q]);
+                    re[q] = fma((double)a.y, (double)b.y, re[q]);
+                    im[q] = fma((double)a.x, (double)b.y, im[q]);
+                    im[q] = fma(-(double)a.y, (double)b.x, im[q]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < KB; ++q) {
+        if (q < kk) {
+            const double2 v = F32 ? make_double2(ff_value(fre[q]), ff_value(fim[q])) : make_double2(re[q], im[q]);
+            const double2 s = block_sum(v);
+            if (threadIdx.x == 0) part[(size_t)(j0 + q) * stride + blockIdx.x] = s;
+        }
+    }
+}
+
+// w += sum_j c_j V_j ; coefficients (complex double) in global memory.
+template <class T2, class A>
+__global__ void mcomb_kernel(const T2* const* __restrict__ V, int k, const double2* __restrict__ c, T2* __restrict__ w,
+                             uint64_t n) {
+    extern __shared__ double2 sc[];
+    for (int j = threadIdx.x; j < k; j += blockDim.x) sc[j] = c[j];
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        T2 o = w[i];
+        A re = (A)o.x, im = (A)o.y;
+        for (int j = 0; j < k; ++j) {
+            const T2 a = V[j][i];
+            const A cr = (A)sc[j].x, ci = (A)sc[j].y;
+            re = fma(cr, (A)a.x, fma(-ci, (A)a.y, re));
+            im = fma(cr, (A)a.y, fma(ci, (A)a.x, im));
+        }
+        o.x = re;
+        o.y = im;
+        w[i] = o;
+    }
+}
+
+__global__ void precond_kernel(const double2* __restrict__ r, const double2* __restrict__ d, double lambda,
+                               double2* __restrict__ t, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        // src/solvers/davidson.cpp:171-175: diff = d_i - lambda, clamped to +-1e-10.
+        double dr = d[i].x - lambda, di = d[i].y;
+        if (sqrt(dr * dr + di * di) < 1e-10) { dr = (dr >= 0) ? 1e-10 : -1e-10; di = 0.0; }
+        const double2 a = r[i];
+        const double den = dr * dr + di * di;
+        t[i] = make_double2((a.x * dr + a.y * di) / den, (a.y * dr - a.x * di) / den);
+    }
+}
+
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw, "Parallel
+// random numbers: as easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64-bit
+// multiplies with the round keys bumped by the Weyl constants.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += W0;
+        k.y += W1;
+    }
+    return c;
+}
+// Element i gets one Philox block; Box-Muller turns its words into a complex
+// standard normal (real and imaginary parts independent N(0,1)).
+template <class T2, bool F64>
+__global__ void philox_normal_kernel(uint64_t seed, uint64_t stream, T2* out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint4 r = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), (uint32_t)stream, (uint32_t)(stream >> 32)),
+                                      make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+        T2 o;
+        if (F64) {
+            const double u1 = ((double)r.x + 1.0) * 2.3283064365386963e-10;  // (0, 1]
+            const double u2 = (double)r.y * 2.3283064365386963e-10;
+            const double rad = sqrt(-2.0 * log(u1));
+            double sn, cs;
+            sincospi(2.0 * u2, &sn, &cs);
+            o.x = rad * cs;
+            o.y = rad * sn;
+        } else {
+            const float u1 = ((float)r.x + 1.0f) * 2.3283064e-10f;
+            const float u2 = (float)r.y * 2.3283064e-10f;
+            const float rad = sqrtf(-2.0f * logf(u1));
+            float sn, cs;
+            sincospif(2.0f * u2, &sn, &cs);
+            o.x = rad * cs;
+            o.y = rad * sn;
+        }
+        out[i] = o;
+    }
+}
+
+double2* finish(Workspace& ws, int nparts, int stride, int k, cudaStream_t s) {
+    finish_kernel<<<k, kThreads, 0, s>>>(ws.partial.as<double2>(), nparts, stride, ws.result.as<double2>());
+    QKG_LAUNCHED();
+    QKG_CUDA(cudaMemcpyAsync(ws.host, ws.result.p, (size_t)k * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    QKG_CUDA(cudaStreamSynchronize(s));
+    return reinterpret_cast<double2*>(ws.host);
+}
+
+}  // namespace
+
+Workspace::Workspace(size_t cap) : cap_partials(cap) {
+    partial.alloc(cap * sizeof(double2));
+    result.alloc(4096 * sizeof(double2));
+    QKG_CUDA(cudaMallocHost(&host, 4096 * sizeof(double2)));
+}
+Workspace::~Workspace() {
+    if (host) cudaFreeHost(host);
+}
+
+std::complex<double> dot_f64(const double2* x, const double2* y, uint64_t n, Workspace& ws, cudaStream_t s) {
+    const int g = stream_grid(n);
+    dot64_kernel<<<g, kThreads, 0, s>>>(x, y, n, ws.partial.as<double2>());
+    QKG_LAUNCHED();
+    const double2 r = finish(ws, g, g, 1, s)[0];
+    return {r.x, r.y};
+}
+std::complex<double> dot_f32(const float2* x, const float2* y, uint64_t n, Workspace& ws, cudaStream_t s) {
+    const int g = stream_grid(n);
+    dot32_kernel<<<g, kThreads, 0, s>>>(x, y, n, ws.partial.as<double2>());
+    QKG_LAUNCHED();
+    const double2 r = finish(ws, g, g, 1, s)[0];
+    return {r.x, r.y};
+}
+double nrm2sq_f64(const double2* x, uint64_t n, Workspace& ws, cudaStream_t s) {
+    const int g = stream_grid(n);
+    nrm64_kernel<<<g, kThreads, 0, s>>>(x, n, ws.partial.as<double2>());
+    QKG_LAUNCHED();
+    return finish(ws, g, g, 1, s)[0].x;
+}
+double nrm2sq_f32(const float2* x, uint64_t n, Workspace& ws, cudaStream_t s) {
+    const int g = stream_grid(n);
+    nrm32_kernel<<<g, kThreads, 0, s>>>(x, n, ws.partial.as<double2>());
+    QKG_LAUNCHED();
+    return finish(ws, g, g, 1, s)[0].x;
+}
+void axpy_f64(std::complex<double> a, const double2* x, double2* y, uint64_t n, cudaStream_t s) {
+    axpy64_kernel<<<stream_grid(n), kThreads, 0, s>>>(a.real(), a.imag(), x, y, n);
+    QKG_LAUNCHED();
+}
+void axpy_f32(std::complex<double> a, const float2* x, float2* y, uint64_t n, cudaStream_t s) {
+    axpy32_kernel<<<stream_grid(n), kThreads, 0, s>>>((float)a.real(), (float)a.imag(), x, y, n);
+    QKG_LAUNCHED();
+}
+void scal_f64(double a, double2* x, uint64_t n, cudaStream_t s) {
+    scal64_kernel<<<stream_grid(n), kThreads, 0, s>>>(a, x, n);
+    QKG_LAUNCHED();
+}
+void scal_f32(double a, float2* x, uint64_t n, cudaStream_t s) {
+    scal32_kernel<<<stream_grid(n), kThreads, 0, s>>>((float)a, x, n);
+    QKG_LAUNCHED();
+}
+void f64_to_f32(const double2* x, float2* y, uint64_t n, cudaStream_t s) {
+    d2f_kernel2<<<stream_grid(n), kThreads, 0, s>>>(x, y, n);
+    QKG_LAUNCHED();
+}
+void f32_to_f64(const float2* x, double2* y, uint64_t n, cudaStream_t s) {
+    f2d_kernel<<<stream_grid(n), kThreads, 0, s>>>(x, y, n);
+    QKG_LAUNCHED();
+}
+double lanczos_update_f64(double2* w, const double2* v, const double2* vp, double alpha, double beta, uint64_t n,
+                          Workspace& ws, cudaStream_t s) {
+    const int g = stream_grid(n);
+    lupd64_kernel<<<g, kThreads, 0, s>>>(w, v, vp, alpha, beta, n, ws.partial.as<double2>());
+    QKG_LAUNCHED();
+    return finish(ws, g, g, 1, s)[0].x;
+}
+double lanczos_update_f32(float2* w, const float2* v, const float2* vp, double alpha, double beta, uint64_t n,
+                          Workspace& ws, cudaStream_t s) {
+    const int g = stream_grid(n);
+    lupd32_kernel<<<g, kThreads, 0, s>>>(w, v, vp, (float)alpha, (float)beta, n, ws.partial.as<double2>());
+    QKG_LAUNCHED();
+    return finish(ws, g, g, 1, s)[0].x;
+}
+
+template <class T2, bool F32>
+static void mdot_impl(const T2* const* V, int k, const T2* w, uint64_t n, std::complex<double>* out, Workspace& ws,
+                      cudaStream_t s) {
+    if (k <= 0) return;
+    QKG_REQUIRE(k <= 4096, "mdot: too many vectors");
+    int g = stream_grid(n);
+    g = (int)std::min<size_t>((size_t)g, ws.cap_partials / (size_t)k);
+    g = std::max(1, g);
+    dim3 grid(g, (k + KB - 1) / KB);
+    mdot_kernel<T2, F32><<<grid, kThreads, 0, s>>>(V, k, w, n, ws.partial.as<double2>(), g);
+    QKG_LAUNCHED();
+    const double2* r = finish(ws, g, g, k, s);
+    for (int j = 0; j < k; ++j) out[j] = {r[j].x, r[j].y};
+}
+void mdot_f64(const double2* const* V, int k, const double2* w, uint64_t n, std::complex<double>* out, Workspace& ws,
+              cudaStream_t s) {
+    mdot_impl<double2, false>(V, k, w, n, out, ws, s);
+}
+void mdot_f32(const float2* const* V, int k, const float2* w, uint64_t n, std::complex<double>* out, Workspace& ws,
+              cudaStream_t s) {
+    mdot_impl<float2, true>(V, k, w, n, out, ws, s);
+}
+
+template <class T2, class A>
+static void mcomb_impl(const T2* const* V, int k, const std::complex<double>* c, T2* w, uint64_t n, Workspace& ws,
+                       cudaStream_t s) {
+    // Chunks of at most 1024 vectors (16 KB of coefficients in shared memory).
+    for (int j0 = 0; j0 < k; j0 += 1024) {
+        const int kk = std::min(1024, k - j0);
+        QKG_CUDA(cudaMemcpyAsync(ws.result.p, c + j0, (size_t)kk * sizeof(double2), cudaMemcpyHostToDevice, s));
+        mcomb_kernel<T2, A><<<stream_grid(n), kThreads, (size_t)kk * sizeof(double2), s>>>(V + j0, kk,
+                                                                                              ws.result.as<double2>(), w, n);
+        QKG_LAUNCHED();
+        QKG_CUDA(cudaStreamSynchronize(s));  // the coefficient slot is reused by the next chunk
+    }
+}
+void mcombine_f64(const double2* const* V, int k, const std::complex<double>* c, double2* w, uint64_t n, Workspace& ws,
+                  cudaStream_t s) {
+    mcomb_impl<double2, double>(V, k, c, w, n, ws, s);
+}
+void mcombine_f32(const float2* const* V, int k, const std::complex<double>* c, float2* w, uint64_t n, Workspace& ws,
+                  cudaStream_t s) {
+    mcomb_impl<float2, float>(V, k, c, w, n, ws, s);
+}
+void philox_normal_f64(uint64_t seed, uint64_t stream, double2* out, uint64_t n, cudaStream_t s) {
+    philox_normal_kernel<double2, true><<<stream_grid(n), kThreads, 0, s>>>(seed, stream, out, n);
+    QKG_LAUNCHED();
+}
+void philox_normal_f32(uint64_t seed, uint64_t stream, float2* out, uint64_t n, cudaStream_t s) {
+    philox_normal_kernel<float2, false><<<stream_grid(n), kThreads, 0, s>>>(seed, stream, out, n);
+    QKG_LAUNCHED();
+}
+void davidson_precond_f64(const double2* r, const double2* d, double lambda, double2* t, uint64_t n, cudaStream_t s) {
+    precond_kernel<<<stream_grid(n), kThreads, 0, s>>>(r, d, lambda, t, n);
+    QKG_LAUNCHED();
+}
+
+}  // namespace qkg

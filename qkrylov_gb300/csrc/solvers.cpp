@@ -1,0 +1,713 @@
+// Solver drivers.  All Krylov vectors stay on the device; the host holds
+// only the small projected problems (tridiagonal / subspace matrices).
+#include "solvers.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <limits>
+#include <numeric>
+#include <random>
+
+namespace qkg {
+
+namespace {
+using clk = std::chrono::steady_clock;
+inline double secs(clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+// A growing list of device vectors plus the device array of their pointers
+// (what the multi-vector kernels take).
+template <class T2>
+struct VecList {
+    uint64_t n = 0;
+    std::vector<DBuf> bufs;
+    std::vector<T2*> host_ptrs;
+    DBuf dev_ptrs;
+    size_t cap = 0;
+    explicit VecList(uint64_t n_) : n(n_) {}
+    T2* push() {
+        size_t fr = 0, tot = 0;
+        QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+        if (fr < n * sizeof(T2) + (64ull << 20))
+            throw Error(CUDA_ERR, "out of device memory for the Krylov basis (" + std::to_string(bufs.size()) + " vectors held)");
+        bufs.emplace_back(n * sizeof(T2));
+        host_ptrs.push_back(bufs.back().as<T2>());
+        sync_ptrs();
+        return host_ptrs.back();
+    }
+    void sync_ptrs() {
+        if (host_ptrs.size() > cap) {
+            cap = std::max<size_t>(64, host_ptrs.size() * 2);
+            dev_ptrs.alloc(cap * sizeof(T2*));
+        }
+        if (!host_ptrs.empty())
+            QKG_CUDA(cudaMemcpy(dev_ptrs.p, host_ptrs.data(), host_ptrs.size() * sizeof(T2*), cudaMemcpyHostToDevice));
+    }
+    void clear() { bufs.clear(); host_ptrs.clear(); }
+    void take(std::vector<DBuf>& nb) {
+        bufs = std::move(nb);
+        host_ptrs.clear();
+        for (auto& b : bufs) host_ptrs.push_back(b.as<T2>());
+        sync_ptrs();
+    }
+    size_t size() const { return host_ptrs.size(); }
+    T2* operator[](size_t i) const { return host_ptrs[i]; }
+    const T2* const* dev() const { return static_cast<const T2* const*>(dev_ptrs.p); }
+};
+
+size_t ws_cap(int k) { return std::max<size_t>(1 << 16, (size_t)1216 * (size_t)std::max(k, 1)); }
+
+void upload_ref_f64(Hamiltonian& H, const cd* host_ref, double2* d_int, DBuf& tmp) {
+    const uint64_t n = H.dim();
+    if (!H.permuted()) {
+        QKG_CUDA(cudaMemcpyAsync(d_int, host_ref, n * sizeof(double2), cudaMemcpyHostToDevice, H.stream()));
+        return;
+    }
+    if (tmp.bytes < n * sizeof(double2)) tmp.alloc(n * sizeof(double2));
+    QKG_CUDA(cudaMemcpyAsync(tmp.p, host_ref, n * sizeof(double2), cudaMemcpyHostToDevice, H.stream()));
+    H.to_internal_f64(tmp.as<double2>(), d_int, H.stream());
+}
+void download_ref_f64(Hamiltonian& H, const double2* d_int, cd* host_ref, DBuf& tmp) {
+    const uint64_t n = H.dim();
+    const double2* src = d_int;
+    if (H.permuted()) {
+        if (tmp.bytes < n * sizeof(double2)) tmp.alloc(n * sizeof(double2));
+        H.to_reference_f64(d_int, tmp.as<double2>(), H.stream());
+        src = tmp.as<double2>();
+    }
+    QKG_CUDA(cudaMemcpyAsync(host_ref, src, n * sizeof(double2), cudaMemcpyDeviceToHost, H.stream()));
+    QKG_CUDA(cudaStreamSynchronize(H.stream()));
+}
+}  // namespace
+
+LaunchTimer::LaunchTimer(cudaStream_t s) : s_(s) {
+    QKG_CUDA(cudaEventCreate(&a_));
+    QKG_CUDA(cudaEventCreate(&b_));
+}
+LaunchTimer::~LaunchTimer() {
+    if (a_) cudaEventDestroy(a_);
+    if (b_) cudaEventDestroy(b_);
+}
+void LaunchTimer::start() { QKG_CUDA(cudaEventRecord(a_, s_)); }
+void LaunchTimer::stop() { QKG_CUDA(cudaEventRecord(b_, s_)); }
+double LaunchTimer::collect() {
+    float ms = 0.0f;
+    QKG_CUDA(cudaEventSynchronize(b_));
+    QKG_CUDA(cudaEventElapsedTime(&ms, a_, b_));
+    return ms * 1e-3;
+}
+
+// ============================================================ small eigenproblems
+double tridiag_lowest(const double* a, const double* b, int n) {
+    if (n <= 0) return 0.0;
+    if (n == 1) return a[0];
+    double lo = std::numeric_limits<double>::infinity(), hi = -lo;
+    for (int i = 0; i < n; ++i) {
+        const double r = (i > 0 ? std::abs(b[i - 1]) : 0.0) + (i < n - 1 ? std::abs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+    }
+    const double scale = std::max(std::abs(lo), std::abs(hi));
+    const double tiny = std::numeric_limits<double>::min() / std::numeric_limits<double>::epsilon();
+    auto count_below = [&](double x) {  // Sturm count: eigenvalues < x
+        int cnt = 0;
+        double q = a[0] - x;
+        if (q < 0) ++cnt;
+        for (int i = 1; i < n; ++i) {
+            if (q == 0.0) q = tiny;
+            q = a[i] - x - b[i - 1] * b[i - 1] / q;
+            if (q < 0) ++cnt;
+        }
+        return cnt;
+    };
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (hi - lo <= 2.0 * std::numeric_limits<double>::epsilon() * scale || mid == lo || mid == hi) break;
+        if (count_below(mid) >= 1) hi = mid;
+        else lo = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// Implicit QL with Wilkinson-type shifts (the symmetric tridiagonal QL of
+// Bowdler, Martin, Reinsch & Wilkinson, Numer. Math. 11 (1968)), rotating only
+// the requested rows of the eigenvector matrix.
+void tridiag_eig(const double* a, const double* b, int n, std::vector<double>& d, const std::vector<int>& rows,
+                 std::vector<double>& z) {
+    d.assign(a, a + n);
+    std::vector<double> e(n, 0.0);
+    for (int i = 0; i + 1 < n; ++i) e[i] = b[i];
+    const int nr = (int)rows.size();
+    z.assign((size_t)nr * n, 0.0);
+    for (int r = 0; r < nr; ++r) if (rows[r] >= 0 && rows[r] < n) z[(size_t)r * n + rows[r]] = 1.0;
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (int l = 0; l < n; ++l) {
+        for (int iter = 0; iter < 100; ++iter) {
+            int m = l;
+            for (; m < n - 1; ++m) {
+                const double dd = std::abs(d[m]) + std::abs(d[m + 1]);
+                if (std::abs(e[m]) <= eps * dd) break;
+            }
+            if (m == l) break;
+            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double r = std::hypot(g, 1.0);
+            g = d[m] - d[l] + e[l] / (g + (g >= 0 ? r : -r));
+            double s = 1.0, c = 1.0, p = 0.0;
+            int i = m - 1;
+            bool underflow = false;
+            for (; i >= l; --i) {
+                const double f = s * e[i], bb = c * e[i];
+                r = std::hypot(f, g);
+                e[i + 1] = r;
+                if (r == 0.0) {
+                    d[i + 1] -= p;
+                    e[m] = 0.0;
+                    underflow = true;
+                    break;
+                }
+                s = f / r;
+                c = g / r;
+                g = d[i + 1] - p;
+                r = (d[i] - g) * s + 2.0 * c * bb;
+                p = s * r;
+                d[i + 1] = g + p;
+                g = c * r - bb;
+                for (int q = 0; q < nr; ++q) {
+                    double* zr = &z[(size_t)q * n];
+                    const double t = zr[i + 1];
+                    zr[i + 1] = s * zr[i] + c * t;
+                    zr[i] = c * zr[i] - s * t;
+                }
+            }
+            if (underflow) continue;
+            d[l] -= p;
+            e[l] = g;
+            e[m] = 0.0;
+        }
+    }
+}
+
+double tridiag_ground(const double* a, const double* b, int n, std::vector<double>& vec) {
+    if (n <= 0) { vec.clear(); return 0.0; }
+    if (n == 1) { vec.assign(1, 1.0); return a[0]; }
+    std::vector<int> rows(n);
+    std::iota(rows.begin(), rows.end(), 0);
+    std::vector<double> d, z;
+    tridiag_eig(a, b, n, d, rows, z);
+    int mi = 0;
+    for (int j = 1; j < n; ++j) if (d[j] < d[mi]) mi = j;
+    vec.resize(n);
+    for (int i = 0; i < n; ++i) vec[i] = z[(size_t)i * n + mi];
+    return d[mi];
+}
+
+void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, std::vector<std::vector<cd>>& vecs) {
+    std::vector<cd> A = H, V((size_t)m * m, 0.0);
+    for (int i = 0; i < m; ++i) V[(size_t)i * m + i] = 1.0;
+    auto at = [&](std::vector<cd>& M, int i, int j) -> cd& { return M[(size_t)i * m + j]; };
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, diag = 0.0;
+        for (int i = 0; i < m; ++i) {
+            diag += std::norm(at(A, i, i));
+            for (int j = i + 1; j < m; ++j) off += std::norm(at(A, i, j));
+        }
+        if (off <= 1e-32 * std::max(diag, 1e-300)) break;
+        for (int p = 0; p < m; ++p)
+            for (int q = p + 1; q < m; ++q) {
+                const cd apq = at(A, p, q);
+                const double mag = std::abs(apq);
+                if (mag < 1e-300) continue;
+                const cd ph = apq / mag;  // e^{i phi}
+                const double app = at(A, p, p).real(), aqq = at(A, q, q).real();
+                const double tau = (aqq - app) / (2.0 * mag);
+                const double t = (tau >= 0 ? 1.0 : -1.0) / (std::abs(tau) + std::sqrt(1.0 + tau * tau));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
+                // U on (p,q): U_pp = c, U_pq = s, U_qp = -s e^{-i phi}, U_qq = c e^{-i phi}
+                const cd upp = c, upq = s, uqp = -s * std::conj(ph), uqq = c * std::conj(ph);
+                for (int k = 0; k < m; ++k) {  // A <- A U, V <- V U
+                    const cd akp = at(A, k, p), akq = at(A, k, q);
+                    at(A, k, p) = akp * upp + akq * uqp;
+                    at(A, k, q) = akp * upq + akq * uqq;
+                    const cd vkp = at(V, k, p), vkq = at(V, k, q);
+                    at(V, k, p) = vkp * upp + vkq * uqp;
+                    at(V, k, q) = vkp * upq + vkq * uqq;
+                }
+                for (int k = 0; k < m; ++k) {  // A <- U^H A
+                    const cd apk = at(A, p, k), aqk = at(A, q, k);
+                    at(A, p, k) = std::conj(upp) * apk + std::conj(uqp) * aqk;
+                    at(A, q, k) = std::conj(upq) * apk + std::conj(uqq) * aqk;
+                }
+                at(A, p, q) = at(A, q, p) = 0.0;
+                at(A, p, p) = at(A, p, p).real();
+                at(A, q, q) = at(A, q, q).real();
+            }
+    }
+    std::vector<int> idx(m);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int i, int j) { return at(A, i, i).real() < at(A, j, j).real(); });
+    evals.clear();
+    vecs.clear();
+    for (int i : idx) {
+        evals.push_back(at(A, i, i).real());
+        std::vector<cd> v(m);
+        for (int k = 0; k < m; ++k) v[k] = at(V, k, i);
+        vecs.push_back(std::move(v));
+    }
+}
+
+// ============================================================ random streams
+void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out) {
+    std::mt19937 rng(seed);
+    std::uniform_real_distribution<double> dist(-1.0, 1.0);
+    for (uint64_t i = 0; i < n; ++i) {
+        const double im = dist(rng);
+        const double re = dist(rng);
+        out[i] = cd(re, im);
+    }
+}
+
+// ============================================================ Lanczos (FP64)
+LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
+    LanczosOut out;
+    const uint64_t n = H.dim();
+    if (n == 0) return out;
+    cudaStream_t st = H.stream();
+    const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
+    Workspace ws(ws_cap(nmax + 2));
+    VecList<double2> V(n);
+    DBuf w(n * sizeof(double2)), tmp;
+    double2* v = V.push();
+    if (o.device_start) {
+        philox_normal_f64(o.seed, 0, v, n, st);
+    } else {
+        std::vector<cd> h(n);
+        if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
+        else ref_uniform_complex(1234, n, h.data());  // src/solvers/lanczos.cpp:115-120
+        upload_ref_f64(H, h.data(), v, tmp);
+    }
+    const double nr0 = std::sqrt(nrm2sq_f64(v, n, ws, st));
+    if (nr0 != 0.0) scal_f64(1.0 / nr0, v, n, st);
+
+    auto& alphas = out.alphas;
+    auto& betas = out.betas;
+    double e_old = 1e100;
+    std::vector<cd> c;
+    LaunchTimer timer(st);
+    const auto t0 = clk::now();
+    for (int iter = 0; iter < nmax; ++iter) {
+        out.iters = iter + 1;
+        v = V[V.size() - 1];
+        const double2* vp = iter > 0 ? V[V.size() - 2] : nullptr;
+        timer.start();
+        H.apply_f64(v, w.as<double2>(), st);
+        timer.stop();
+        const double alpha = dot_f64(v, w.as<double2>(), n, ws, st).real();  // synchronises the stream
+        out.t_spmv += timer.collect();
+        ++out.n_spmv;
+        alphas.push_back(alpha);
+        lanczos_update_f64(w.as<double2>(), v, vp, alpha, iter > 0 ? betas.back() : 0.0, n, ws, st);
+        // full reorthogonalisation against every stored vector (:148-151), one CGS pass
+        const int k = (int)V.size();
+        c.assign(k, 0.0);
+        mdot_f64(V.dev(), k, w.as<double2>(), n, c.data(), ws, st);
+        for (auto& x : c) x = -x;
+        mcombine_f64(V.dev(), k, c.data(), w.as<double2>(), n, ws, st);
+        const double beta = std::sqrt(nrm2sq_f64(w.as<double2>(), n, ws, st));
+        if (beta < 1e-15) { out.converged = true; break; }
+        if (iter + 1 == nmax) break;
+        betas.push_back(beta);
+        double2* vn = V.push();
+        QKG_CUDA(cudaMemcpyAsync(vn, w.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal_f64(1.0 / beta, vn, n, st);
+        if (iter > 0 && !o.fixed_steps) {
+            const double e = tridiag_lowest(alphas.data(), betas.data(), (int)alphas.size());
+            if (std::abs(e - e_old) < o.tol) { out.converged = true; break; }
+            e_old = e;
+        }
+    }
+    QKG_CUDA(cudaStreamSynchronize(st));
+    out.t_loop = secs(t0, clk::now());
+    std::vector<double> s;
+    out.energy = tridiag_ground(alphas.data(), betas.data(), (int)alphas.size(), s);
+    out.energy_tridiag = out.energy;
+    out.residual = -1.0;
+    if (o.want_vec) {
+        DBuf ritz(n * sizeof(double2));
+        QKG_CUDA(cudaMemsetAsync(ritz.p, 0, n * sizeof(double2), st));
+        std::vector<cd> cc(s.size());
+        for (size_t i = 0; i < s.size(); ++i) cc[i] = s[i];
+        mcombine_f64(V.dev(), (int)s.size(), cc.data(), ritz.as<double2>(), n, ws, st);
+        const double nr = std::sqrt(nrm2sq_f64(ritz.as<double2>(), n, ws, st));
+        if (nr != 0.0) scal_f64(1.0 / nr, ritz.as<double2>(), n, st);
+        out.evec.resize(n);
+        download_ref_f64(H, ritz.as<double2>(), out.evec.data(), tmp);
+    }
+    return out;
+}
+
+// ============================================================ Lanczos (mixed)
+LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
+    LanczosOut out;
+    const uint64_t n = H.dim();
+    if (n == 0) return out;
+    cudaStream_t st = H.stream();
+    const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
+    Workspace ws(ws_cap(nmax + 2));
+    VecList<float2> V(n);
+    VecList<float2> psi(n);  // converged Ritz vectors used for selective reorthogonalisation
+    DBuf w(n * sizeof(float2)), tmp;
+    float2* v = V.push();
+    if (o.device_start) {
+        philox_normal_f32(o.seed, 0, v, n, st);
+    } else {
+        std::vector<cd> h(n);
+        if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
+        else ref_uniform_complex(1234, n, h.data());
+        DBuf d64(n * sizeof(double2));
+        upload_ref_f64(H, h.data(), d64.as<double2>(), tmp);
+        f64_to_f32(d64.as<double2>(), v, n, st);
+    }
+    const double nr0 = std::sqrt(nrm2sq_f32(v, n, ws, st));
+    if (nr0 != 0.0) scal_f32(1.0 / nr0, v, n, st);
+
+    auto& alphas = out.alphas;
+    auto& betas = out.betas;
+    double e_old = 1e100;
+    std::vector<cd> c;
+    const double so_tol = 3.5e-4;  // sqrt(eps_fp32): Parlett-Scott selective-orthogonalisation threshold
+    LaunchTimer timer(st);
+    const auto t0 = clk::now();
+    for (int iter = 0; iter < nmax; ++iter) {
+        out.iters = iter + 1;
+        v = V[V.size() - 1];
+        const float2* vp = iter > 0 ? V[V.size() - 2] : nullptr;
+        timer.start();
+        H.apply_f32(v, w.as<float2>(), st);
+        timer.stop();
+        const double alpha = dot_f32(v, w.as<float2>(), n, ws, st).real();  // synchronises the stream
+        out.t_spmv += timer.collect();
+        ++out.n_spmv;
+        alphas.push_back(alpha);
+        double b2 = lanczos_update_f32(w.as<float2>(), v, vp, alpha, iter > 0 ? betas.back() : 0.0, n, ws, st);
+        if (psi.size()) {
+            c.assign(psi.size(), 0.0);
+            mdot_f32(psi.dev(), (int)psi.size(), w.as<float2>(), n, c.data(), ws, st);
+            for (auto& x : c) x = -x;
+            mcombine_f32(psi.dev(), (int)psi.size(), c.data(), w.as<float2>(), n, ws, st);
+            b2 = nrm2sq_f32(w.as<float2>(), n, ws, st);
+            ++out.n_selective;
+        }
+        const double beta = std::sqrt(b2);
+        if (beta < 1e-15) { out.converged = true; break; }
+        if (iter + 1 == nmax) break;
+        betas.push_back(beta);
+        float2* vn = V.push();
+        QKG_CUDA(cudaMemcpyAsync(vn, w.p, n * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+        scal_f32(1.0 / beta, vn, n, st);
+        const int k = (int)alphas.size();
+        if (iter > 0) {
+            const double e = tridiag_lowest(alphas.data(), betas.data(), k);
+            if (!o.fixed_steps && std::abs(e - e_old) < o.tol) { out.converged = true; break; }
+            e_old = e;
+            // Selective reorthogonalisation: once the lowest Ritz pair has
+            // converged to FP32 level (|beta_k s_k| <= sqrt(eps) ||T||), keep
+            // later Lanczos vectors orthogonal to its Ritz vector.
+            if (psi.size() == 0 && k >= 4) {
+                std::vector<double> d, z;
+                tridiag_eig(alphas.data(), betas.data(), k, d, {k - 1}, z);
+                int mi = 0;
+                for (int j = 1; j < k; ++j) if (d[j] < d[mi]) mi = j;
+                double tn = 0.0;
+                for (int j = 0; j < k; ++j) tn = std::max(tn, std::abs(d[j]));
+                if (beta * std::abs(z[mi]) <= so_tol * tn) {
+                    std::vector<double> s;
+                    tridiag_ground(alphas.data(), betas.data(), k, s);
+                    float2* p = psi.push();
+                    QKG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(float2), st));
+                    std::vector<cd> cc(s.begin(), s.end());
+                    V.sync_ptrs();
+                    mcombine_f32(V.dev(), k, cc.data(), p, n, ws, st);
+                    const double pn = std::sqrt(nrm2sq_f32(p, n, ws, st));
+                    scal_f32(1.0 / pn, p, n, st);
+                    // the newest Lanczos vector is also made orthogonal to it
+                    std::complex<double> cp = -dot_f32(p, vn, n, ws, st);
+                    axpy_f32(cp, p, vn, n, st);
+                    const double vnn = std::sqrt(nrm2sq_f32(vn, n, ws, st));
+                    scal_f32(1.0 / vnn, vn, n, st);
+                }
+            }
+        }
+    }
+    QKG_CUDA(cudaStreamSynchronize(st));
+    out.t_loop = secs(t0, clk::now());
+    const auto t1 = clk::now();
+    std::vector<double> s;
+    out.energy_tridiag = tridiag_ground(alphas.data(), betas.data(), (int)alphas.size(), s);
+    // Ritz vector from the FP32 basis, then FP64 Rayleigh quotient and residual.
+    DBuf r32(n * sizeof(float2)), r64(n * sizeof(double2)), h64(n * sizeof(double2));
+    QKG_CUDA(cudaMemsetAsync(r32.p, 0, n * sizeof(float2), st));
+    std::vector<cd> cc(s.begin(), s.end());
+    mcombine_f32(V.dev(), (int)s.size(), cc.data(), r32.as<float2>(), n, ws, st);
+    f32_to_f64(r32.as<float2>(), r64.as<double2>(), n, st);
+    const double nr = std::sqrt(nrm2sq_f64(r64.as<double2>(), n, ws, st));
+    scal_f64(1.0 / nr, r64.as<double2>(), n, st);
+    H.apply_f64(r64.as<double2>(), h64.as<double2>(), st);
+    const double E = dot_f64(r64.as<double2>(), h64.as<double2>(), n, ws, st).real();
+    axpy_f64(-E, r64.as<double2>(), h64.as<double2>(), n, st);
+    out.residual = std::sqrt(nrm2sq_f64(h64.as<double2>(), n, ws, st));
+    out.energy = E;
+    out.t_refine = secs(t1, clk::now());
+    if (o.want_vec) {
+        out.evec.resize(n);
+        download_ref_f64(H, r64.as<double2>(), out.evec.data(), tmp);
+    }
+    return out;
+}
+
+// ============================================================ continued fraction
+CFOut cf_f64(Hamiltonian& H, const cd* phi0_ref, int n_iter) {
+    CFOut out;
+    const uint64_t n = H.dim();
+    if (n == 0) return out;
+    cudaStream_t st = H.stream();
+    Workspace ws(ws_cap(2));
+    DBuf a(n * sizeof(double2)), b(n * sizeof(double2)), w(n * sizeof(double2)), tmp;
+    double2 *v = a.as<double2>(), *vp = b.as<double2>();
+    upload_ref_f64(H, phi0_ref, v, tmp);
+    const double np = std::sqrt(nrm2sq_f64(v, n, ws, st));
+    if (np < 1e-15) return out;  // src/solvers/dynamics.cpp:26
+    scal_f64(1.0 / np, v, n, st);
+    out.norm = np;
+    for (int it = 0; it < n_iter; ++it) {
+        H.apply_f64(v, w.as<double2>(), st);
+        const double alpha = dot_f64(v, w.as<double2>(), n, ws, st).real();
+        out.alphas.push_back(alpha);
+        const double b2 = lanczos_update_f64(w.as<double2>(), v, it > 0 ? vp : nullptr, alpha,
+                                             it > 0 ? out.betas.back() : 0.0, n, ws, st);
+        const double beta = std::sqrt(b2);
+        if (beta < 1e-15) break;
+        out.betas.push_back(beta);
+        // rotate: vp <- v, v <- w / beta, w <- old vp buffer
+        std::swap(vp, v);
+        double2* wp = w.as<double2>();
+        QKG_CUDA(cudaMemcpyAsync(v, wp, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal_f64(1.0 / beta, v, n, st);
+    }
+    QKG_CUDA(cudaStreamSynchronize(st));
+    return out;
+}
+
+// Backward continued fraction at z = omega + E0 + i eta (dynamics.cpp:61-89).
+double spectral(const double* alphas, const double* betas, size_t n, double norm, double omega, double E0, double eta) {
+    if (n == 0) return 0.0;
+    const cd z(omega + E0, eta);
+    cd f = 0.0;
+    for (int i = (int)n - 1; i >= 0; --i) {
+        if (i == (int)n - 1) f = 1.0 / (z - alphas[i]);
+        else f = 1.0 / (z - alphas[i] - betas[i] * betas[i] * f);
+    }
+    return -1.0 / M_PI * std::imag(norm * norm * f);
+}
+
+// ============================================================ FTLM
+std::vector<FTLMTri> ftlm_tridiags_f64(Hamiltonian& H, int n_random, int n_steps) {
+    std::vector<FTLMTri> out;
+    const uint64_t n = H.dim();
+    if (n == 0 || n_random <= 0) return out;
+    cudaStream_t st = H.stream();
+    Workspace ws(ws_cap(2));
+    DBuf a(n * sizeof(double2)), b(n * sizeof(double2)), w(n * sizeof(double2)), tmp;
+    std::mt19937 rng(42);  // src/solvers/ftlm.cpp:133-134: one stream across all vectors
+    std::normal_distribution<double> dist(0.0, 1.0);
+    std::vector<cd> h(n);
+    for (int r = 0; r < n_random; ++r) {
+        for (uint64_t i = 0; i < n; ++i) {
+            const double im = dist(rng);
+            const double re = dist(rng);
+            h[i] = cd(re, im);
+        }
+        double2 *v = a.as<double2>(), *vp = b.as<double2>();
+        upload_ref_f64(H, h.data(), v, tmp);
+        FTLMTri t;
+        t.norm2 = nrm2sq_f64(v, n, ws, st);
+        const double nr = std::sqrt(t.norm2);
+        if (nr != 0.0) scal_f64(1.0 / nr, v, n, st);
+        std::vector<double> al, be;
+        for (int i = 0; i < n_steps; ++i) {
+            H.apply_f64(v, w.as<double2>(), st);
+            const double alpha = dot_f64(v, w.as<double2>(), n, ws, st).real();
+            al.push_back(alpha);
+            const double b2 = lanczos_update_f64(w.as<double2>(), v, i > 0 ? vp : nullptr, alpha, i > 0 ? be.back() : 0.0,
+                                                 n, ws, st);
+            const double beta = std::sqrt(b2);
+            if (beta < 1e-15) break;
+            be.push_back(beta);
+            std::swap(vp, v);
+            QKG_CUDA(cudaMemcpyAsync(v, w.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            scal_f64(1.0 / beta, v, n, st);
+        }
+        std::vector<double> z;
+        tridiag_eig(al.data(), be.data(), (int)al.size(), t.evals, {0}, z);
+        t.w0.resize(t.evals.size());
+        for (size_t j = 0; j < t.evals.size(); ++j) t.w0[j] = z[j] * z[j];
+        out.push_back(std::move(t));
+    }
+    return out;
+}
+
+// Z, E, Cv at each beta (ftlm.cpp:151-167).  With `shifted`, weights use
+// exp(-beta (e - e_min)) and log_zmax[b] = -beta e_min, so that Z = Zs e^{log_zmax}
+// stays finite where exp(-beta e) overflows.
+void ftlm_observables(const std::vector<FTLMTri>& tri, const double* betas, int nb, double* Zo, double* Eo, double* Co,
+                      bool shifted, double* log_zmax) {
+    double emin = std::numeric_limits<double>::infinity();
+    for (const auto& t : tri) for (double e : t.evals) emin = std::min(emin, e);
+    const int R = (int)tri.size();
+    for (int k = 0; k < nb; ++k) {
+        const double beta = betas[k];
+        const double sh = shifted ? emin : 0.0;
+        double Z = 0, E = 0, E2 = 0;
+        for (const auto& t : tri)
+            for (size_t i = 0; i < t.evals.size(); ++i) {
+                const double wgt = t.norm2 * t.w0[i] * std::exp(-beta * (t.evals[i] - sh));
+                Z += wgt;
+                E += t.evals[i] * wgt;
+                E2 += t.evals[i] * t.evals[i] * wgt;
+            }
+        if (R > 0) { Z /= R; E /= R; E2 /= R; }
+        Zo[k] = Z;
+        Eo[k] = E / Z;
+        Co[k] = beta * beta * (E2 / Z - (E / Z) * (E / Z));
+        if (log_zmax) log_zmax[k] = shifted ? -beta * emin : 0.0;
+    }
+}
+
+// ============================================================ Davidson
+DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs) {
+    DavidsonOut out;
+    const uint64_t n = H.dim();
+    if (n == 0) return out;
+    cudaStream_t st = H.stream();
+    n_eig = (int)std::min<uint64_t>((uint64_t)n_eig, n);
+    max_sub = std::max(max_sub, 2 * n_eig);
+    Workspace ws(ws_cap(max_sub + n_eig + 2));
+    DBuf diag(n * sizeof(double2)), tmp;
+    H.diagonal_f64(diag.as<double2>(), st);
+    // Seeds: unit vectors at the n_eig smallest diagonal entries, in the order
+    // std::sort leaves them (davidson.cpp:111-121); the diagonal is taken in the
+    // reference's order so ties resolve as they do there.
+    const std::vector<cd> dref = H.diagonal_host_ref();
+    std::vector<uint64_t> di(n);
+    std::iota(di.begin(), di.end(), 0);
+    if (n <= (1ull << 23)) {
+        std::sort(di.begin(), di.end(), [&](uint64_t i, uint64_t j) { return dref[i].real() < dref[j].real(); });
+    } else {
+        std::partial_sort(di.begin(), di.begin() + n_eig, di.end(), [&](uint64_t i, uint64_t j) {
+            return dref[i].real() < dref[j].real() || (dref[i].real() == dref[j].real() && i < j);
+        });
+    }
+    std::mt19937 rng(1234);
+    std::uniform_real_distribution<double> dist(-1.0, 1.0);
+    VecList<double2> V(n), HV(n);
+    std::vector<cd> hv(n), c;
+    auto orthonormalize = [&](double2* t) -> double {
+        if (V.size()) {
+            c.assign(V.size(), 0.0);
+            mdot_f64(V.dev(), (int)V.size(), t, n, c.data(), ws, st);
+            for (auto& x : c) x = -x;
+            mcombine_f64(V.dev(), (int)V.size(), c.data(), t, n, ws, st);
+        }
+        return std::sqrt(nrm2sq_f64(t, n, ws, st));
+    };
+    DBuf seed(n * sizeof(double2));
+    for (int i = 0; i < n_eig; ++i) {
+        std::fill(hv.begin(), hv.end(), cd(0.0));
+        hv[di[i]] = 1.0;
+        upload_ref_f64(H, hv.data(), seed.as<double2>(), tmp);
+        double nrm = orthonormalize(seed.as<double2>());
+        if (nrm < 1e-10) {
+            for (uint64_t j = 0; j < n; ++j) { const double im = dist(rng); const double re = dist(rng); hv[j] = cd(re, im); }
+            upload_ref_f64(H, hv.data(), seed.as<double2>(), tmp);
+            nrm = orthonormalize(seed.as<double2>());
+        }
+        double2* v = V.push();
+        QKG_CUDA(cudaMemcpyAsync(v, seed.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal_f64(1.0 / nrm, v, n, st);
+        H.apply_f64(v, HV.push(), st);
+    }
+    DBuf r(n * sizeof(double2));
+    for (int iter = 0; iter < 100; ++iter) {
+        const int m = (int)V.size();
+        std::vector<cd> Hs((size_t)m * m);
+        std::vector<cd> col(m);
+        for (int j = 0; j < m; ++j) {
+            mdot_f64(V.dev(), m, HV[j], n, col.data(), ws, st);  // <V_i, HV_j>
+            for (int i = j; i < m; ++i) {
+                Hs[(size_t)i * m + j] = col[i];
+                if (i != j) Hs[(size_t)j * m + i] = std::conj(col[i]);
+            }
+        }
+        std::vector<double> ev;
+        std::vector<std::vector<cd>> evec;
+        hermitian_eig(Hs, m, ev, evec);
+        bool all_conv = true;
+        std::vector<DBuf> corr;
+        for (int k = 0; k < n_eig; ++k) {
+            const double lambda = ev[k];
+            QKG_CUDA(cudaMemsetAsync(r.p, 0, n * sizeof(double2), st));
+            std::vector<cd> cs(evec[k]), cl(m);
+            for (int i = 0; i < m; ++i) cl[i] = -lambda * evec[k][i];
+            mcombine_f64(HV.dev(), m, cs.data(), r.as<double2>(), n, ws, st);
+            mcombine_f64(V.dev(), m, cl.data(), r.as<double2>(), n, ws, st);
+            const double rn = std::sqrt(nrm2sq_f64(r.as<double2>(), n, ws, st));
+            if (rn > tol) {
+                all_conv = false;
+                DBuf t(n * sizeof(double2));
+                davidson_precond_f64(r.as<double2>(), diag.as<double2>(), lambda, t.as<double2>(), n, st);
+                corr.push_back(std::move(t));
+            }
+        }
+        if (all_conv || iter == 99) {
+            out.iters = iter + 1;
+            out.converged = all_conv;
+            DBuf e(n * sizeof(double2));
+            for (int k = 0; k < n_eig; ++k) {
+                out.evals.push_back(ev[k]);
+                if (want_vecs) {
+                    QKG_CUDA(cudaMemsetAsync(e.p, 0, n * sizeof(double2), st));
+                    mcombine_f64(V.dev(), m, evec[k].data(), e.as<double2>(), n, ws, st);
+                    std::vector<cd> h(n);
+                    download_ref_f64(H, e.as<double2>(), h.data(), tmp);
+                    out.evecs.push_back(std::move(h));
+                }
+            }
+            QKG_CUDA(cudaStreamSynchronize(st));
+            return out;
+        }
+        if (V.size() + corr.size() > (size_t)max_sub) {  // restart to the Ritz vectors (:196-211)
+            std::vector<DBuf> nv, nh;
+            for (int k = 0; k < n_eig; ++k) {
+                nv.emplace_back(n * sizeof(double2));
+                nh.emplace_back(n * sizeof(double2));
+                QKG_CUDA(cudaMemsetAsync(nv.back().p, 0, n * sizeof(double2), st));
+                QKG_CUDA(cudaMemsetAsync(nh.back().p, 0, n * sizeof(double2), st));
+                mcombine_f64(V.dev(), m, evec[k].data(), nv.back().as<double2>(), n, ws, st);
+                mcombine_f64(HV.dev(), m, evec[k].data(), nh.back().as<double2>(), n, ws, st);
+            }
+            V.take(nv);
+            HV.take(nh);
+        }
+        for (auto& t : corr) {  // orthogonalise each correction and extend (:213-223)
+            const double nrm = orthonormalize(t.as<double2>());
+            if (nrm > 1e-10) {
+                scal_f64(1.0 / nrm, t.as<double2>(), n, st);
+                double2* v = V.push();
+                QKG_CUDA(cudaMemcpyAsync(v, t.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+                H.apply_f64(v, HV.push(), st);
+            }
+        }
+    }
+    return out;
+}
+
+}  // namespace qkg

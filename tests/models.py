@@ -69,11 +69,15 @@ def fermion_chain_terms(L, pbc, t=1.0, V=0.7, mu=0.3):
 
 
 def xyz_field_terms(L, pbc, hx=0.3, hy=0.2, cplx=0.1):
-    """Spin terms that leave the Sz sector (Sx, Sy) and carry complex coefficients."""
+    """Hermitian spin model with terms that leave the Sz sector (Sx, Sy) and
+    complex coefficients on conjugate pairs (a Dzyaloshinskii-Moriya-like bond)."""
     terms = heisenberg_terms(L, pbc)
     for i in range(L):
         terms.append((hx, [("Sx", i)]))
-        terms.append((complex(hy, cplx), [("Sy", i)]))
+        terms.append((hy, [("Sy", i)]))
+    for i in range(0, L - 1, 2):
+        terms.append((complex(0.0, cplx), [("Sp", i), ("Sm", i + 1)]))
+        terms.append((complex(0.0, -cplx), [("Sm", i), ("Sp", i + 1)]))
     terms.append((0.1, [("Sz", 0), ("Sz", 1), ("Sz", 2)]))
     terms.append((complex(0.2, -0.05), [("Sp", 0), ("Sz", 1), ("Sm", 2)]))
     terms.append((complex(0.2, 0.05), [("Sm", 0), ("Sz", 1), ("Sp", 2)]))

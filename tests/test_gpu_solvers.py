@@ -1,0 +1,155 @@
+"""GPU solvers against the reference: Lanczos E0 within 1e-10 relative,
+Davidson eigenvalues, continued-fraction coefficients and S(omega), FTLM
+tridiagonals and Z/E/Cv within 1e-8, and the mixed form's |dE0| against FP64."""
+import numpy as np
+import pytest
+
+import models as M
+from conftest import golden_names, golden_terms, load_golden, make_model
+from oracle_ctypes import OHam, spectral
+
+pytestmark = pytest.mark.gpu
+
+E0_RTOL = 1e-10    # spec bar for E0 against the reference's FP64 Lanczos
+DYN_RTOL = 1e-8    # S(omega), FTLM Z/E/Cv
+
+
+def gpu_ham(qk, g):
+    basis, site, ops = make_model(qk, g["model"], g["nsites"], g["sector"], golden_terms(g))
+    return qk.MatrixFreeHamiltonian(basis, site, ops)
+
+
+def hermitian(name):
+    return True
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_lanczos_energy(qk, name):
+    g = load_golden(name)
+    H = gpu_ham(qk, g)
+    r = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12)
+    e_ref = float(g["lanczos_E0"])
+    assert abs(r.energy - e_ref) <= E0_RTOL * max(1.0, abs(e_ref))
+    assert r.converged
+    assert abs(r.iterations - int(g["lanczos_iters"])) <= 3
+    v = r.eigenvector
+    assert abs(np.linalg.norm(v) - 1) < 1e-12
+    res = np.linalg.norm(H.apply(v) - r.energy * v)
+    assert res < 1e-6
+
+
+def test_configs0_heisenberg_L16_obc(qk):
+    """configs[0]: L=16 open chain, Sz=0, tol 1e-12, <=300 iterations; the
+    reference gives E0 = -6.911737145574688 (golden heis_L16_obc_sz0)."""
+    g = load_golden("heis_L16_obc_sz0")
+    H = gpu_ham(qk, g)
+    r = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12)
+    assert abs(r.energy - float(g["lanczos_E0"])) <= E0_RTOL * abs(float(g["lanczos_E0"]))
+    assert abs(r.energy - (-6.911737145574688)) < 1e-10 * 6.92
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_davidson(qk, name):
+    g = load_golden(name)
+    H = gpu_ham(qk, g)
+    k = len(g["davidson_evals"])
+    r = qk.davidson_lowest(H, n_eig=k, max_subspace=20, tol=1e-8)
+    if bool(g["davidson_conv"]):
+        assert r.converged
+        np.testing.assert_allclose(r.eigenvalues, g["davidson_evals"], rtol=1e-8, atol=1e-8)
+        for lam, v in zip(r.eigenvalues, r.eigenvectors):
+            assert np.linalg.norm(H.apply(v) - lam * v) <= 1e-6
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if n != "heis_L16_obc_sz0"])
+def test_continued_fraction(qk, name):
+    g = load_golden(name)
+    H = gpu_ham(qk, g)
+    r = qk.continued_fraction_coeffs(H, g["cf_phi0"], len(g["cf_alphas"]))
+    assert abs(r.norm_phi0 - float(g["cf_norm"])) <= 1e-13 * float(g["cf_norm"])
+    k = min(10, len(r.alphas))
+    np.testing.assert_allclose(r.alphas[:k], g["cf_alphas"][:k], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(r.betas[:k], g["cf_betas"][:k], rtol=1e-9, atol=1e-9)
+    # S(omega) from the first 10 coefficients on a grid, same formula as dynamics.cpp:61-89
+    om = np.linspace(0.0, 4.0, 41)
+    res10 = qk.DynamicsResult(r.alphas[:k], r.betas[:k], r.norm_phi0)
+    s_gpu = qk.evaluate_spectral_function(res10, om, E0=-1.0, eta=0.05)
+    ref10 = qk.DynamicsResult(g["cf_alphas"][:k], g["cf_betas"][:k], float(g["cf_norm"]))
+    s_ref = qk.evaluate_spectral_function(ref10, om, E0=-1.0, eta=0.05)
+    np.testing.assert_allclose(s_gpu, s_ref, rtol=DYN_RTOL, atol=DYN_RTOL * np.abs(s_ref).max())
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_ftlm(qk, name):
+    g = load_golden(name)
+    H = gpu_ham(qk, g)
+    R, Mst = g["ftlm_alphas"].shape
+    r = qk.ftlm(H, g["ftlm_betas_T"], n_random=R, n_steps=Mst)
+    obs = g["ftlm_obs"]
+    np.testing.assert_allclose(r.partition_function, obs[:, 0], rtol=DYN_RTOL)
+    np.testing.assert_allclose(r.internal_energy, obs[:, 1], rtol=DYN_RTOL, atol=DYN_RTOL)
+    np.testing.assert_allclose(r.specific_heat, obs[:, 2], rtol=DYN_RTOL, atol=DYN_RTOL)
+    # shifted evaluation gives the same values after undoing the shift
+    s = qk.ftlm(H, g["ftlm_betas_T"], n_random=R, n_steps=Mst, shifted=True)
+    np.testing.assert_allclose(s.partition_function * np.exp(s.log_shift), obs[:, 0], rtol=DYN_RTOL)
+    np.testing.assert_allclose(s.internal_energy, obs[:, 1], rtol=DYN_RTOL, atol=DYN_RTOL)
+
+
+def test_reference_known_answers(qk):
+    # tests/test_lanczos_ritz.cpp: 2 sites, full basis, E0 = -0.75, Ritz residual < 1e-5
+    b, s, o = make_model(qk, M.SPIN, 2, M.sector(), M.heisenberg_terms(2, False))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    r = qk.lanczos_ground_state(H)
+    assert abs(r.energy + 0.75) < 1e-5
+    assert np.abs(H.apply(r.eigenvector) - r.energy * r.eigenvector).max() < 1e-5
+    # bindings/julia/test/runtests.jl:122: periodic 4-site chain, full basis, E0 = -2
+    b, s, o = make_model(qk, M.SPIN, 4, M.sector(), M.heisenberg_terms(4, True))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    assert abs(qk.lanczos_ground_state(H, maxiter=50, tol=1e-12).energy + 2.0) < 1e-6
+    r2 = qk.lanczos_ground_state(H, maxiter=2, tol=1e-15)
+    assert not r2.converged and r2.iterations == 2
+    # tests/test_ftlm.cpp: H = Sz0 Sz1 on 2 sites, Z > 0, |E| < 1
+    b, s, o = make_model(qk, M.SPIN, 2, M.sector(), [(1.0, [("Sz", 0), ("Sz", 1)])])
+    f = qk.ftlm(qk.MatrixFreeHamiltonian(b, s, o), 1.0, 100, 10)
+    assert f.partition_function > 0 and abs(f.internal_energy) < 1
+    # tests/test_dynamics.cpp: S(0.5) >= 0 from phi0 = e_0
+    b, s, o = make_model(qk, M.SPIN, 2, M.sector(), M.heisenberg_terms(2, False))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    e0 = qk.lanczos_ground_state(H).energy
+    phi0 = np.zeros(4, dtype=complex)
+    phi0[0] = 1
+    d = qk.continued_fraction_coeffs(H, phi0, 10)
+    assert len(d.alphas) > 0 and qk.evaluate_spectral_function(d, 0.5, e0, 0.1) >= 0
+
+
+@pytest.mark.parametrize("L", [16, 20])
+def test_mixed_form_matches_fp64(qk, L):
+    """Mixed form: |dE0| <= 1e-10 relative against the FP64 path."""
+    b, s, o = make_model(qk, M.SPIN, L, M.sector(sz2=0), M.heisenberg_terms(L, True))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    r64 = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12)
+    rm = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12, mixed=True)
+    assert abs(rm.energy - r64.energy) <= 1e-10 * abs(r64.energy)
+    assert rm.residual < 1e-4
+    ov = abs(np.vdot(rm.eigenvector, r64.eigenvector))
+    assert ov > 1 - 1e-8
+
+
+def test_lanczos_from_given_start_matches_oracle(qk, oracle):
+    """Same start vector on both sides: E0 and iteration count of the
+    reference algorithm (oracle restatement) are reproduced."""
+    m = M.hubbard(6, True, 3, 3)
+    b, s, o = make_model(qk, *m)
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    oh = OHam(oracle, *m)
+    rng = np.random.default_rng(11)
+    v0 = rng.normal(size=oh.dim) + 1j * rng.normal(size=oh.dim)
+    r = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12, v0=v0)
+    import ctypes as c
+    e, it, cv = c.c_double(), c.c_int(), c.c_int()
+    evec = np.zeros(oh.dim, dtype=complex)
+    oracle.lib.qko_lanczos_from(c.c_void_p(oh.h), v0.ctypes.data_as(c.POINTER(c.c_double)), 300, c.c_double(1e-12),
+                                c.byref(e), c.byref(it), c.byref(cv), evec.ctypes.data_as(c.POINTER(c.c_double)),
+                                None, None)
+    assert abs(r.energy - e.value) <= E0_RTOL * abs(e.value)
+    assert abs(abs(np.vdot(r.eigenvector, evec)) - 1) < 1e-8
