@@ -389,6 +389,7 @@ int qkrylov_lanczos_ground_state_complex(qkrylov_hamiltonian_h h, int maxiter, f
         o.maxiter = maxiter;
         o.tol = (double)tol;
         o.want_vec = ev != nullptr;
+        o.f32_stream = true;  // the reference's C API runs its FP32 engine
         const auto res = qkg::lanczos_f64(*h->ptr, o);
         r->energy = (float)res.energy;
         r->iterations = res.iters;
@@ -457,7 +458,7 @@ int qkrylov_davidson_lowest_complex(qkrylov_hamiltonian_h h, int n_eig, int max_
     if (!h || !h->ptr || !evals || n_eig <= 0) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         set_device(h);
-        const auto res = qkg::davidson_f64(*h->ptr, n_eig, max_sub, (double)tol, evecs != nullptr);
+        const auto res = qkg::davidson_f64(*h->ptr, n_eig, max_sub, (double)tol, evecs != nullptr, true);
         const size_t k = std::min<size_t>((size_t)n_eig, res.evals.size());
         for (size_t i = 0; i < k; ++i) evals[i] = (float)res.evals[i];
         if (info) { info->iterations = res.iters; info->converged = res.converged ? 1 : 0; }
@@ -537,15 +538,20 @@ int qkrylov_evaluate_spectral_grid_f64(const double* alphas, const double* betas
 
 int qkrylov_ftlm(qkrylov_hamiltonian_h h, float beta, int n_random, int n_steps, qkrylov_ftlm_result_c_t* r) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;
-    qkrylov_ftlm_result_f64_t d;
-    const int rc = qkrylov_ftlm_f64(h, (double)beta, n_random, n_steps, &d);
-    if (rc == QKRYLOV_SUCCESS) {
-        r->beta = (float)d.beta;
-        r->partition_function = (float)d.partition_function;
-        r->internal_energy = (float)d.internal_energy;
-        r->specific_heat = (float)d.specific_heat;
-    }
-    return rc;
+    return guarded([&] {
+        set_device(h);
+        r->beta = beta;
+        r->partition_function = r->internal_energy = r->specific_heat = 0.0f;
+        if (h->ptr->dim() == 0) return;
+        // random vectors as the reference's FP32 engine draws them (normal_distribution<float>)
+        const auto tri = qkg::ftlm_tridiags_f64(*h->ptr, n_random, n_steps, true);
+        const double b = (double)beta;
+        double Z, E, C;
+        qkg::ftlm_observables(tri, &b, 1, &Z, &E, &C, false, nullptr);
+        r->partition_function = (float)Z;
+        r->internal_energy = (float)E;
+        r->specific_heat = (float)C;
+    });
 }
 int qkrylov_ftlm_f64(qkrylov_hamiltonian_h h, double beta, int n_random, int n_steps, qkrylov_ftlm_result_f64_t* r) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;

@@ -256,13 +256,37 @@ void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, 
 }
 
 // ============================================================ random streams
-void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out) {
-    std::mt19937 rng(seed);
-    std::uniform_real_distribution<double> dist(-1.0, 1.0);
+namespace {
+template <class Dist>
+void fill_stream(std::mt19937& rng, Dist& dist, uint64_t n, cd* out) {
     for (uint64_t i = 0; i < n; ++i) {
-        const double im = dist(rng);
+        const double im = dist(rng);  // g++ evaluates the imaginary argument first
         const double re = dist(rng);
         out[i] = cd(re, im);
+    }
+}
+// One random stream across all vectors (src/solvers/ftlm.cpp:133-143).
+struct NormalStream {
+    std::mt19937 rng{42};
+    std::normal_distribution<double> d64{0.0, 1.0};
+    std::normal_distribution<float> d32{0.0f, 1.0f};
+    bool f32;
+    explicit NormalStream(bool f) : f32(f) {}
+    void fill(uint64_t n, cd* out) {
+        if (f32) fill_stream(rng, d32, n, out);
+        else fill_stream(rng, d64, n, out);
+    }
+};
+}  // namespace
+
+void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out, bool f32) {
+    std::mt19937 rng(seed);
+    if (f32) {
+        std::uniform_real_distribution<float> dist(-1.0f, 1.0f);
+        fill_stream(rng, dist, n, out);
+    } else {
+        std::uniform_real_distribution<double> dist(-1.0, 1.0);
+        fill_stream(rng, dist, n, out);
     }
 }
 
@@ -282,7 +306,7 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
     } else {
         std::vector<cd> h(n);
         if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
-        else ref_uniform_complex(1234, n, h.data());  // src/solvers/lanczos.cpp:115-120
+        else ref_uniform_complex(1234, n, h.data(), o.f32_stream);  // src/solvers/lanczos.cpp:115-120
         upload_ref_f64(H, h.data(), v, tmp);
     }
     const double nr0 = std::sqrt(nrm2sq_f64(v, n, ws, st));
@@ -510,22 +534,17 @@ double spectral(const double* alphas, const double* betas, size_t n, double norm
 }
 
 // ============================================================ FTLM
-std::vector<FTLMTri> ftlm_tridiags_f64(Hamiltonian& H, int n_random, int n_steps) {
+std::vector<FTLMTri> ftlm_tridiags_f64(Hamiltonian& H, int n_random, int n_steps, bool f32_stream) {
     std::vector<FTLMTri> out;
     const uint64_t n = H.dim();
     if (n == 0 || n_random <= 0) return out;
     cudaStream_t st = H.stream();
     Workspace ws(ws_cap(2));
     DBuf a(n * sizeof(double2)), b(n * sizeof(double2)), w(n * sizeof(double2)), tmp;
-    std::mt19937 rng(42);  // src/solvers/ftlm.cpp:133-134: one stream across all vectors
-    std::normal_distribution<double> dist(0.0, 1.0);
+    NormalStream stream(f32_stream);  // mt19937(42), src/solvers/ftlm.cpp:133-134
     std::vector<cd> h(n);
     for (int r = 0; r < n_random; ++r) {
-        for (uint64_t i = 0; i < n; ++i) {
-            const double im = dist(rng);
-            const double re = dist(rng);
-            h[i] = cd(re, im);
-        }
+        stream.fill(n, h.data());
         double2 *v = a.as<double2>(), *vp = b.as<double2>();
         upload_ref_f64(H, h.data(), v, tmp);
         FTLMTri t;
@@ -583,7 +602,7 @@ void ftlm_observables(const std::vector<FTLMTri>& tri, const double* betas, int 
 }
 
 // ============================================================ Davidson
-DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs) {
+DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream) {
     DavidsonOut out;
     const uint64_t n = H.dim();
     if (n == 0) return out;
@@ -596,7 +615,9 @@ DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, boo
     // Seeds: unit vectors at the n_eig smallest diagonal entries, in the order
     // std::sort leaves them (davidson.cpp:111-121); the diagonal is taken in the
     // reference's order so ties resolve as they do there.
-    const std::vector<cd> dref = H.diagonal_host_ref();
+    std::vector<cd> dref = H.diagonal_host_ref();
+    if (f32_stream)  // the FP32 engine sorts its float diagonal
+        for (auto& d : dref) d = cd((double)(float)d.real(), 0.0);
     std::vector<uint64_t> di(n);
     std::iota(di.begin(), di.end(), 0);
     if (n <= (1ull << 23)) {
@@ -608,6 +629,7 @@ DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, boo
     }
     std::mt19937 rng(1234);
     std::uniform_real_distribution<double> dist(-1.0, 1.0);
+    std::uniform_real_distribution<float> dist32(-1.0f, 1.0f);
     VecList<double2> V(n), HV(n);
     std::vector<cd> hv(n), c;
     auto orthonormalize = [&](double2* t) -> double {
@@ -626,7 +648,8 @@ DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, boo
         upload_ref_f64(H, hv.data(), seed.as<double2>(), tmp);
         double nrm = orthonormalize(seed.as<double2>());
         if (nrm < 1e-10) {
-            for (uint64_t j = 0; j < n; ++j) { const double im = dist(rng); const double re = dist(rng); hv[j] = cd(re, im); }
+            if (f32_stream) fill_stream(rng, dist32, n, hv.data());
+            else fill_stream(rng, dist, n, hv.data());
             upload_ref_f64(H, hv.data(), seed.as<double2>(), tmp);
             nrm = orthonormalize(seed.as<double2>());
         }

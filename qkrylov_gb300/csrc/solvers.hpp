@@ -29,7 +29,9 @@ void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, 
 // Filled as the reference fills KComplex(dist(rng), dist(rng)) when compiled
 // with g++, which evaluates the imaginary (second) argument first
 // (src/solvers/lanczos.cpp:115-120, ftlm.cpp:133-143, davidson.cpp:106-128).
-void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out);
+// `f32` draws through the float distributions, as the reference's FP32 engine
+// (the one behind its C API, where Real = float) does.
+void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out, bool f32 = false);
 // Device Philox4x32-10 (Salmon et al., SC'11) Gaussian complex vectors.
 void philox_normal_f64(uint64_t seed, uint64_t stream, double2* out, uint64_t n, cudaStream_t s);
 void philox_normal_f32(uint64_t seed, uint64_t stream, float2* out, uint64_t n, cudaStream_t s);
@@ -43,6 +45,7 @@ struct LanczosOpts {
     bool fixed_steps = false;    // run exactly maxiter steps (no early exit on |dE| < tol)
     bool device_start = false;   // seeded Philox Gaussian start (performance runs)
     uint64_t seed = 0;
+    bool f32_stream = false;     // draw the start vector as the reference's FP32 engine does
 };
 struct LanczosOut {
     double energy = 0.0;       // reported energy (refined for the mixed form)
@@ -90,12 +93,12 @@ struct FTLMTri {  // per random vector
     std::vector<double> evals, w0;  // eigenvalues and squared first components
     double norm2 = 0.0;             // ||r||^2 of the un-normalised random vector
 };
-std::vector<FTLMTri> ftlm_tridiags_f64(Hamiltonian& H, int n_random, int n_steps);
+std::vector<FTLMTri> ftlm_tridiags_f64(Hamiltonian& H, int n_random, int n_steps, bool f32_stream = false);
 void ftlm_observables(const std::vector<FTLMTri>& tri, const double* betas, int nb, double* Z, double* E, double* Cv,
                       bool shifted, double* log_zmax);
 
 // ---- Davidson (src/solvers/davidson.cpp:86-227) -------------------------------
 struct DavidsonOut { std::vector<double> evals; std::vector<std::vector<cd>> evecs; int iters = 0; bool converged = false; };
-DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs);
+DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream = false);
 
 }  // namespace qkg

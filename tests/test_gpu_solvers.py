@@ -19,10 +19,6 @@ def gpu_ham(qk, g):
     return qk.MatrixFreeHamiltonian(basis, site, ops)
 
 
-def hermitian(name):
-    return True
-
-
 @pytest.mark.parametrize("name", golden_names())
 def test_lanczos_energy(qk, name):
     g = load_golden(name)
@@ -34,8 +30,10 @@ def test_lanczos_energy(qk, name):
     assert abs(r.iterations - int(g["lanczos_iters"])) <= 3
     v = r.eigenvector
     assert abs(np.linalg.norm(v) - 1) < 1e-12
+    # |dE| < tol stops the iteration with a residual of order sqrt(tol);
+    # the reference's own Ritz test bounds it by 1e-5 (tests/test_lanczos_ritz.cpp:52-55)
     res = np.linalg.norm(H.apply(v) - r.energy * v)
-    assert res < 1e-6
+    assert res < 1e-5
 
 
 def test_configs0_heisenberg_L16_obc(qk):
