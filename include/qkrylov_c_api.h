@@ -243,6 +243,17 @@ int qkrylov_ftlm_multi_beta_f64(qkrylov_hamiltonian_h h, const double* betas, in
 int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* n_outer, int* n_inner, int* n_mixed, int* n_diag,
                              int* diag_mode);
 
+/* SpMV kernel choice: generic = 0 lets the library use its table-driven fast
+ * kernel when the Hamiltonian qualifies (32-bit states, coded diagonal);
+ * generic = 1 forces the generic kernel.  *fast_in_use (optional) reports the
+ * kernel that applies from now on. */
+int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use);
+
+/* Time `reps` back-to-back applies of the FP32 (fp32 != 0) or FP64 kernel on
+ * internal device vectors, with CUDA events on the Hamiltonian's stream;
+ * *ms_per_apply receives the mean launch duration. */
+int qkrylov_hamiltonian_benchmark_apply(qkrylov_hamiltonian_h h, int fp32, int reps, double* ms_per_apply);
+
 /* Every generated matrix entry, rows and columns in the reference's order and
  * entries of a row in OpSum term order -- the content of the reference's CSR
  * (matrix_free_hamiltonian.cpp:45-92).  Call once with row_offsets = cols =

@@ -113,6 +113,8 @@ _SIGS = {
     "qkrylov_ftlm_multi_beta_f64": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, _dp, _dp]),
     "qkrylov_hamiltonian_info": (_i, [_vp, _ip, _ip, _ip, _ip, _ip]),
     "qkrylov_hamiltonian_entries": (_i, [_vp, _u64p, _u64p, _u64p, _dp]),
+    "qkrylov_hamiltonian_select_kernel": (_i, [_vp, _i, _ip]),
+    "qkrylov_hamiltonian_benchmark_apply": (_i, [_vp, _i, _i, _dp]),
 }
 
 _lib = None
@@ -345,6 +347,19 @@ class MatrixFreeHamiltonian(_Handle):
         v = [_c.c_int() for _ in range(5)]
         _check(lib().qkrylov_hamiltonian_info(self._h, *[_c.byref(x) for x in v]))
         return dict(zip(["n_outer", "n_inner", "n_mixed", "n_diag", "diag_mode"], [x.value for x in v]))
+
+    def select_kernel(self, generic=False):
+        """Force the generic SpMV kernel (True) or allow the fast one (False);
+        returns whether the fast kernel is in use."""
+        f = _c.c_int()
+        _check(lib().qkrylov_hamiltonian_select_kernel(self._h, int(bool(generic)), _c.byref(f)))
+        return bool(f.value)
+
+    def benchmark_apply(self, fp32=True, reps=10):
+        """Mean CUDA-event duration (ms) of one apply of the selected kernel."""
+        ms = _c.c_double()
+        _check(lib().qkrylov_hamiltonian_benchmark_apply(self._h, int(bool(fp32)), int(reps), _c.byref(ms)))
+        return ms.value
 
     def entries(self):
         """(row_offsets, cols, vals) of every generated entry, reference order."""

@@ -345,6 +345,39 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* no, int* ni, int* nm,
     return QKRYLOV_SUCCESS;
 }
 
+int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use) {
+    if (!h || !h->ptr) return QKRYLOV_ERROR_INVALID_ARG;
+    h->ptr->force_generic(generic != 0);
+    if (fast_in_use) *fast_in_use = h->ptr->fast() ? 1 : 0;
+    return QKRYLOV_SUCCESS;
+}
+
+int qkrylov_hamiltonian_benchmark_apply(qkrylov_hamiltonian_h h, int fp32, int reps, double* ms) {
+    if (!h || !h->ptr || !ms || reps <= 0) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        set_device(h);
+        auto& H = *h->ptr;
+        const uint64_t n = H.dim();
+        *ms = 0.0;
+        if (!n) return;
+        cudaStream_t s = H.stream();
+        const size_t e = fp32 ? sizeof(float2) : sizeof(double2);
+        qkg::DBuf x(n * e), y(n * e);
+        if (fp32) qkg::philox_normal_f32(7, 0, x.as<float2>(), n, s);
+        else qkg::philox_normal_f64(7, 0, x.as<double2>(), n, s);
+        auto run = [&] {
+            if (fp32) H.apply_f32(x.as<float2>(), y.as<float2>(), s);
+            else H.apply_f64(x.as<double2>(), y.as<double2>(), s);
+        };
+        run();  // warm-up
+        qkg::LaunchTimer t(s);
+        t.start();
+        for (int r = 0; r < reps; ++r) run();
+        t.stop();
+        *ms = 1e3 * t.collect() / reps;
+    });
+}
+
 int qkrylov_hamiltonian_entries(qkrylov_hamiltonian_h h, uint64_t* nnz_out, uint64_t* ro, uint64_t* cols, double* vals) {
     if (!h || !h->ptr || !nnz_out) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {

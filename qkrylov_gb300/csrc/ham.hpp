@@ -76,10 +76,26 @@ public:
     int n_diag() const { return t64_.n_diag; }
     int diag_mode() const { return diag_mode_; }
     size_t n_items() const { return n_items_; }
+    bool fast() const { return fast_ && !force_generic_; }
+    void force_generic(bool on) { force_generic_ = on; }
+    size_t inner_table_entries() const { return n_ient_; }
 
 private:
     void build_diagonal();
+    void build_fast();
     template <class S> void upload_terms(const std::vector<HostTerm>& ht);
+
+    // fast-path data (see spmv_fast_kernel)
+    struct FastSet {
+        DBuf outer, inner, mixed, vars;
+        int n_outer = 0, n_inner = 0, n_mixed = 0, outer_has_j = 0;
+    };
+    bool fast_ = false, force_generic_ = false, unif_ = false;
+    double u_ar_ = 0.0, u_ai_ = 0.0;
+    int rbits_ = 0;
+    size_t n_ient_ = 0;
+    FastSet f64s_, f32s_;
+    DBuf iptr_, ient_;
 
     std::shared_ptr<Basis> basis_;
     const DevBasis* db_ = nullptr;

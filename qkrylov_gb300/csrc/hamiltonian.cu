@@ -48,6 +48,7 @@ namespace {
 constexpr int kBlock = 256;
 constexpr uint32_t kChunk = 1024;
 constexpr int kMaxOuter = 256;
+constexpr int kMaxInnerTable = 512;  // inner terms a table may reference
 constexpr size_t kSmemTermBudget = 40 * 1024;
 
 template <class S, class A>
@@ -300,6 +301,165 @@ __global__ void __launch_bounds__(kBlock) spmv_kernel(const SpmvParams<S, A> p, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fast path (32-bit states, table ranks, 32-bit indices, coded diagonal).
+//
+// Inner terms are replaced by a table built once per Hamiltonian: for every
+// inner configuration b (indexed like inner_state, so consecutive rows of a
+// work item read consecutive table rows) the list of (target inner rank,
+// amplitude index) of the inner terms valid on b, in term order, with their
+// Jordan-Wigner sign folded in.  The table depends only on b, so one copy
+// serves every block.  Outer terms become a per-block list in shared memory;
+// the remaining (straddling) terms are evaluated generically.
+template <class A>
+struct alignas(16) OutEnt {
+    int32_t delta;
+    uint32_t J;
+    A ar, ai;
+};
+
+template <class A>
+struct FastParams {
+    int n_in;
+    uint32_t in_mask;
+    int ngroups, no_double, N;
+    uint32_t gmask0, gmask1;
+    int gpop0, gpop1;
+    const uint32_t* outer_off;
+    const uint32_t* inner_rank;   // null: inner rank = inner bits
+    const uint32_t* inner_state;  // null: inner configuration = table index
+    const WorkItem* items;
+    const uint32_t* iptr;         // table rows
+    const uint32_t* ient;         // entries: rank | inner sign << rbits | term << (rbits + 1)
+    int rbits;
+    const KTerm<uint32_t, A>* inner;  // per term: amplitude, J (its outer part signs per block)
+    int n_inner;
+    A u_ar, u_ai;                 // UNIF: the one amplitude (no signs)
+    const KTerm<uint32_t, A>* outer;
+    int n_outer, outer_has_j;
+    const KTerm<uint32_t, A>* mixed;
+    const KVar<A>* vars;
+    int n_mixed;
+    int diag_mode;
+    const void* dcode;
+    const A* dtab;
+};
+
+__device__ __forceinline__ bool in_basis_fast(int ng, uint32_t g0, uint32_t g1, int p0, int p1, int no_double, int N,
+                                              uint32_t s) {
+    if (ng > 0 && __popc(s & g0) != p0) return false;
+    if (ng > 1 && __popc(s & g1) != p1) return false;
+    if (no_double && (s & (s >> N) & ((1u << N) - 1u))) return false;
+    return true;
+}
+
+template <class T, class A, bool REAL, bool UNIF>
+__global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x,
+                                                           typename V2<T>::t* __restrict__ y) {
+    using T2 = typename V2<T>::t;
+    __shared__ OutEnt<A> s_out[kMaxOuter];
+    __shared__ A s_iamp[2 * kMaxInnerTable];
+    __shared__ int s_n;
+    const WorkItem it = p.items[blockIdx.x];
+    const uint32_t block_off = __ldg(p.outer_off + it.a);
+    if (!UNIF) {
+        // inner-term amplitudes with the sign their JW mask takes on this block's outer bits
+        const uint32_t sa = it.a << p.n_in;
+        for (int t = threadIdx.x; t < p.n_inner; t += blockDim.x) {
+            const KTerm<uint32_t, A> k = p.inner[t];
+            const bool neg = __popc(sa & k.J) & 1;
+            s_iamp[2 * t] = neg ? -k.ar : k.ar;
+            s_iamp[2 * t + 1] = neg ? -k.ai : k.ai;
+        }
+    }
+    if (threadIdx.x < 32) {
+        // the outer terms valid for this block, in term order
+        const uint32_t b0 = p.inner_state ? __ldg(p.inner_state + it.inner_base) : it.inner_base;
+        const uint32_t s0 = (it.a << p.n_in) | b0;
+        int base = 0;
+        for (int t0 = 0; t0 < p.n_outer; t0 += 32) {
+            const int ti = t0 + (int)threadIdx.x;
+            bool ok = false;
+            OutEnt<A> e;
+            if (ti < p.n_outer) {
+                const KTerm<uint32_t, A> t = p.outer[ti];
+                if ((s0 & t.C) == t.V) {
+                    const uint32_t s2 = s0 ^ t.X;
+                    if (!(t.flags & 1u) || in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2)) {
+                        ok = true;
+                        e.delta = (int32_t)(__ldg(p.outer_off + (s2 >> p.n_in)) - block_off);
+                        e.J = t.J;
+                        e.ar = t.ar;
+                        e.ai = t.ai;
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) s_out[base + __popc(m & ((1u << threadIdx.x) - 1u))] = e;
+            base += __popc(m);
+        }
+        if (threadIdx.x == 0) s_n = base;
+    }
+    __syncthreads();
+    const int nout = s_n;
+    for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
+        const uint32_t row = (uint32_t)it.row0 + r;
+        const uint32_t pidx = it.inner_base + r;
+        const uint32_t b = p.inner_state ? __ldg(p.inner_state + pidx) : pidx;
+        const uint32_t s = (it.a << p.n_in) | b;
+        A accr, acci;
+        {
+            const uint32_t c = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
+                                                      : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
+            const A dr = __ldg(p.dtab + 2 * c);
+            const T2 xv = x[row];
+            accr = dr * (A)xv.x;
+            acci = dr * (A)xv.y;
+            if (!REAL) {
+                const A di = __ldg(p.dtab + 2 * c + 1);
+                accr = fma(-di, (A)xv.y, accr);
+                acci = fma(di, (A)xv.x, acci);
+            }
+        }
+        for (int k = 0; k < nout; ++k) {
+            const OutEnt<A> e = s_out[k];
+            const T2 xv = x[row + e.delta];
+            const A sg = (__popc(s & e.J) & 1) ? (A)-1 : (A)1;
+            cmac<A>(accr, acci, sg * e.ar, sg * e.ai, xv, REAL);
+        }
+        const uint32_t e0 = __ldg(p.iptr + pidx), e1 = __ldg(p.iptr + pidx + 1);
+        const uint32_t rmask = (1u << p.rbits) - 1u;
+#pragma unroll 4
+        for (uint32_t e = e0; e < e1; ++e) {
+            const uint32_t ent = __ldg(p.ient + e);
+            const T2 xv = x[block_off + (ent & rmask)];
+            if (UNIF) {
+                cmac<A>(accr, acci, p.u_ar, p.u_ai, xv, REAL);
+            } else {
+                const uint32_t t = ent >> (p.rbits + 1);
+                const A sg = ((ent >> p.rbits) & 1u) ? (A)-1 : (A)1;
+                cmac<A>(accr, acci, sg * s_iamp[2 * t], sg * s_iamp[2 * t + 1], xv, REAL);
+            }
+        }
+        for (int k = 0; k < p.n_mixed; ++k) {
+            const KTerm<uint32_t, A> t = p.mixed[k];
+            if ((s & t.C) != t.V) continue;
+            const uint32_t s2 = s ^ t.X;
+            if ((t.flags & 1u) && !in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2))
+                continue;
+            const uint32_t b2 = s2 & p.in_mask;
+            const uint32_t idx = __ldg(p.outer_off + (s2 >> p.n_in)) + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+            A ar, ai;
+            term_amp<uint32_t, A>(t, s, p.vars, ar, ai);
+            cmac<A>(accr, acci, ar, ai, x[idx], REAL);
+        }
+        T2 out;
+        out.x = (T)accr;
+        out.y = (T)acci;
+        y[row] = out;
+    }
+}
+
 // Diagonal of H, summed in OpSum term order like the reference
 // (matrix_free_hamiltonian.cpp:86-89).
 template <class S, int RANK>
@@ -485,6 +645,137 @@ Hamiltonian::Hamiltonian(std::shared_ptr<Basis> basis, SiteKind site, const std:
     upload_vec(items_, items);
     QKG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     build_diagonal();
+    build_fast();
+}
+
+namespace {
+template <class S, class A>
+void pack(const std::vector<const HostTerm*>& lst, std::vector<KTerm<S, A>>& out, std::vector<KVar<A>>& vars) {
+    for (const HostTerm* h : lst) {
+        out.push_back(to_kterm<S, A>(*h, (uint32_t)vars.size()));
+        for (const DVar& v : h->vars) vars.push_back({v.sm, v.pf, (A)v.a0r, (A)v.a0i, (A)v.a1r, (A)v.a1i});
+    }
+}
+}  // namespace
+
+void Hamiltonian::build_fast() {
+    const Basis& B = *basis_;
+    fast_ = false;
+    if (B.rank_kind != RANK_TABLE || wide_ || dim() == 0 || dim() >= (1ull << 31) || diag_mode_ == DIAG_FULL) return;
+    const uint64_t inm = db_->in_mask;
+    std::vector<const HostTerm*> outer, inner, mixed;
+    for (const auto& h : hterms_) {
+        if (h.X == 0) continue;
+        if (((h.X | h.C) & ~inm) == 0 && h.vars.empty()) inner.push_back(&h);
+        else if (((h.X | h.C) & inm) == 0 && h.vars.empty()) outer.push_back(&h);
+        else mixed.push_back(&h);
+    }
+    if ((int)outer.size() > kMaxOuter) { mixed.insert(mixed.end(), outer.begin(), outer.end()); outer.clear(); }
+    if ((int)inner.size() > kMaxInnerTable) { mixed.insert(mixed.end(), inner.begin(), inner.end()); inner.clear(); }
+    // Inner table over all inner configurations of the classes that occur.
+    const uint32_t P = 1u << B.n_in;
+    std::vector<char> present(B.n_in + 2, B.inner_all ? 1 : 0);
+    if (!B.inner_all)
+        for (uint64_t a = 0; a < (1ull << B.n_out); ++a)
+            if (B.outer_off[a + 1] > B.outer_off[a]) present[B.inner_class_of((uint32_t)a)] = 1;
+    rbits_ = std::max(1, B.n_in);
+    const int tbits = 32 - rbits_ - 1;
+    if (tbits < 1 || (inner.size() > (1ull << tbits))) return;
+    std::vector<uint32_t> ptr(P + 1, 0), ent;
+    unif_ = true;
+    const std::complex<double> amp0 = inner.empty() ? std::complex<double>(0.0) : inner[0]->amp;
+    for (const HostTerm* h : inner)
+        if (h->amp != amp0 || (h->J != 0)) unif_ = false;
+    for (uint32_t pi = 0; pi < P; ++pi) {
+        ptr[pi] = (uint32_t)ent.size();
+        const uint32_t b = B.inner_all ? pi : B.inner_state[pi];
+        if (!B.inner_all && !present[__builtin_popcount(b)]) continue;
+        for (size_t t = 0; t < inner.size(); ++t) {
+            const HostTerm& h = *inner[t];
+            if ((b & h.C) != h.V) continue;
+            const uint32_t b2 = b ^ (uint32_t)h.X;
+            // an inner flip stays in the sector iff the inner popcount class is kept
+            if (h.check && !B.inner_all && __builtin_popcount(b2) != __builtin_popcount(b)) continue;
+            const uint32_t r2 = B.inner_all ? b2 : B.inner_rank[b2];
+            const uint32_t sg = __builtin_popcountll((uint64_t)b & h.J & inm) & 1u;
+            ent.push_back(r2 | (sg << rbits_) | ((uint32_t)t << (rbits_ + 1)));
+        }
+        if (ent.size() > (1ull << 30)) return;
+    }
+    ptr[P] = (uint32_t)ent.size();
+    n_ient_ = ent.size();
+    upload_vec(iptr_, ptr);
+    upload_vec(ient_, ent);
+    u_ar_ = amp0.real();
+    u_ai_ = amp0.imag();
+    auto build = [&](auto tag, FastSet& fs) {
+        using A = decltype(tag);
+        std::vector<KTerm<uint32_t, A>> ko, ki, km;
+        std::vector<KVar<A>> vars, dummy;
+        pack<uint32_t, A>(outer, ko, dummy);
+        pack<uint32_t, A>(inner, ki, dummy);
+        pack<uint32_t, A>(mixed, km, vars);
+        upload_vec(fs.outer, ko);
+        upload_vec(fs.inner, ki);
+        upload_vec(fs.mixed, km);
+        upload_vec(fs.vars, vars);
+        fs.n_outer = (int)ko.size();
+        fs.n_inner = (int)ki.size();
+        fs.n_mixed = (int)km.size();
+        fs.outer_has_j = 0;
+        for (const auto* h : outer) if (h->J) fs.outer_has_j = 1;
+    };
+    build(double(), f64s_);
+    build(float(), f32s_);
+    fast_ = true;
+}
+
+template <class T, class A>
+static void launch_fast(const DevBasis& b, const DBuf& items, size_t n_items, const DBuf& iptr, const DBuf& ient,
+                        int rbits, bool unif, double uar, double uai, const DBuf& outer, int n_outer, int outer_has_j,
+                        const DBuf& inner, int n_inner, const DBuf& mixed, const DBuf& vars, int n_mixed, bool real,
+                        int diag_mode, const DBuf& dcode, const DBuf& dtab, const typename V2<T>::t* x,
+                        typename V2<T>::t* y, cudaStream_t s) {
+    if (!n_items) return;
+    FastParams<A> p;
+    p.n_in = b.n_in;
+    p.in_mask = (uint32_t)b.in_mask;
+    p.ngroups = b.ngroups;
+    p.no_double = b.no_double;
+    p.N = b.N;
+    p.gmask0 = (uint32_t)b.gmask[0];
+    p.gmask1 = (uint32_t)b.gmask[1];
+    p.gpop0 = b.gpop[0];
+    p.gpop1 = b.gpop[1];
+    p.outer_off = static_cast<const uint32_t*>(b.outer_off);
+    p.inner_rank = b.inner_all ? nullptr : b.inner_rank;
+    p.inner_state = b.inner_all ? nullptr : b.inner_state;
+    p.items = items.as<WorkItem>();
+    p.iptr = iptr.as<uint32_t>();
+    p.ient = ient.as<uint32_t>();
+    p.rbits = rbits;
+    p.inner = inner.as<KTerm<uint32_t, A>>();
+    p.n_inner = n_inner;
+    p.u_ar = (A)uar;
+    p.u_ai = (A)uai;
+    p.outer = outer.as<KTerm<uint32_t, A>>();
+    p.n_outer = n_outer;
+    p.outer_has_j = outer_has_j;
+    p.mixed = mixed.as<KTerm<uint32_t, A>>();
+    p.vars = vars.as<KVar<A>>();
+    p.n_mixed = n_mixed;
+    p.diag_mode = diag_mode;
+    p.dcode = dcode.p;
+    p.dtab = dtab.as<A>();
+    const unsigned g = (unsigned)n_items;
+    if (real) {
+        if (unif) spmv_fast_kernel<T, A, true, true><<<g, kBlock, 0, s>>>(p, x, y);
+        else spmv_fast_kernel<T, A, true, false><<<g, kBlock, 0, s>>>(p, x, y);
+    } else {
+        if (unif) spmv_fast_kernel<T, A, false, true><<<g, kBlock, 0, s>>>(p, x, y);
+        else spmv_fast_kernel<T, A, false, false><<<g, kBlock, 0, s>>>(p, x, y);
+    }
+    QKG_LAUNCHED();
 }
 
 Hamiltonian::~Hamiltonian() {
@@ -599,6 +890,12 @@ static void launch_spmv(const DevBasis& b, const TermSet& ts, const DBuf& items,
 }
 
 void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const {
+    if (fast()) {
+        launch_fast<double, double>(*db_, items_, n_items_, iptr_, ient_, rbits_, unif_, u_ar_, u_ai_, f64s_.outer,
+                                    f64s_.n_outer, f64s_.outer_has_j, f64s_.inner, f64s_.n_inner, f64s_.mixed,
+                                    f64s_.vars, f64s_.n_mixed, all_real_, diag_mode_, dcode_, dtab64_, x, y, s);
+        return;
+    }
     const DBuf& full = dfull64_;
     if (wide_)
         launch_spmv<uint64_t, double, double>(*db_, t64_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab64_, full, x, y, s);
@@ -607,6 +904,12 @@ void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const 
 }
 
 void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
+    if (fast()) {
+        launch_fast<float, float>(*db_, items_, n_items_, iptr_, ient_, rbits_, unif_, u_ar_, u_ai_, f32s_.outer,
+                                  f32s_.n_outer, f32s_.outer_has_j, f32s_.inner, f32s_.n_inner, f32s_.mixed, f32s_.vars,
+                                  f32s_.n_mixed, all_real_, diag_mode_, dcode_, dtab32_, x, y, s);
+        return;
+    }
     if (wide_)
         launch_spmv<uint64_t, float, float>(*db_, t32_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab32_, dfull32_, x, y, s);
     else

@@ -83,10 +83,12 @@ def test_entries_bit_exact(qk, name):
     np.testing.assert_allclose(vals, g["csr_vals"], rtol=0, atol=1e-15)
 
 
+@pytest.mark.parametrize("generic", [False, True], ids=["fast", "generic"])
 @pytest.mark.parametrize("name", golden_names())
-def test_apply_and_diagonal(qk, name):
+def test_apply_and_diagonal(qk, name, generic):
     g = load_golden(name)
     H = gpu_ham(qk, g)
+    H.select_kernel(generic)
     assert H.dimension == int(g["dim"])
     np.testing.assert_array_equal(H.diagonal(), g["diag"].real)  # summed in term order: bit-exact
     if "x" in g:
@@ -95,6 +97,15 @@ def test_apply_and_diagonal(qk, name):
         assert np.abs(y - g["y"]).max() <= RTOL64 * scale
         y32 = apply32(qk, H, g["x"])
         assert np.abs(y32 - g["y"]).max() <= RTOL32 * scale * 10
+
+
+def test_fast_kernel_is_used_where_eligible(qk):
+    for m in (M.heisenberg(16, True, 0), M.hubbard(8, True, 4, 4), (M.SPIN, 12, M.sector(), M.xyz_field_terms(12, True)),
+              (M.FERMION, 14, M.sector(n=5), M.fermion_chain_terms(14, True))):
+        b, s, o = make_model(qk, *m)
+        H = qk.MatrixFreeHamiltonian(b, s, o)
+        assert H.select_kernel(False), m[:3]
+        assert not H.select_kernel(True)
 
 
 @pytest.mark.parametrize("model,N,sector,terms", [
@@ -114,10 +125,12 @@ def test_apply_against_oracle(qk, oracle, model, N, sector, terms):
     rng = np.random.default_rng(7)
     x = rng.normal(size=o.dim) + 1j * rng.normal(size=o.dim)
     yo = o.apply(x)
-    y = H.apply(x)
-    assert np.abs(y - yo).max() <= RTOL64 * np.abs(yo).max()
-    y32 = apply32(qk, H, x)
-    assert np.abs(y32 - yo).max() <= RTOL32 * 10 * np.abs(yo).max()
+    for generic in (False, True):
+        H.select_kernel(generic)
+        y = H.apply(x)
+        assert np.abs(y - yo).max() <= RTOL64 * np.abs(yo).max()
+        y32 = apply32(qk, H, x)
+        assert np.abs(y32 - yo).max() <= RTOL32 * 10 * np.abs(yo).max()
 
 
 def test_edge_cases(qk):
