@@ -167,6 +167,16 @@ int qkrylov_hamiltonian_diagonal_f64(qkrylov_hamiltonian_h h, double* diag_out /
 int qkrylov_hamiltonian_apply_device_f64(qkrylov_hamiltonian_h h, const void* d_x, void* d_y, void* stream);
 int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* d_x, void* d_y, void* stream);
 
+/* <x, y> = sum_i conj(x_i) y_i of two device vectors of n complex elements
+ * (interleaved), run on `stream` (NULL = legacy default stream) on the current
+ * GPU; result[0], result[1] (host) receive the real and imaginary parts, and
+ * the call synchronises the stream.  The reference's dot (include/qkrylov/
+ * linalg/vector_ops.hpp:14-32) returned a host scalar the same way.  The _f32
+ * form reduces FP32 data with compensated (FP64-accurate) arithmetic.  Scratch
+ * for the partial sums is allocated by the library on first use. */
+int qkrylov_vector_dot_device_f64(const void* d_x, const void* d_y, uint64_t n, double* result, void* stream);
+int qkrylov_vector_dot_device_f32(const void* d_x, const void* d_y, uint64_t n, double* result, void* stream);
+
 /* Lanczos ground state, FP64 (reference semantics: full reorthogonalisation,
  * stop when |E_k - E_{k-1}| < tol; lanczos.cpp:101-202).  The start vector is
  * the reference's (mt19937(1234), uniform[-1,1] complex) unless v0 (dim complex,

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <mutex>
 
 #include "solvers.hpp"
 
@@ -87,6 +88,18 @@ void apply_host_f64(qkrylov_hamiltonian_h h, const double* x, double* y) {
     H.to_reference_f64(h->y64.as<double2>(), h->t64.as<double2>(), s);
     QKG_CUDA(cudaMemcpyAsync(y, h->t64.p, n * sizeof(double2), cudaMemcpyDeviceToHost, s));
     QKG_CUDA(cudaStreamSynchronize(s));
+}
+
+// One reduction workspace per GPU for the device-vector BLAS calls.
+qkg::Workspace& device_workspace() {
+    static std::mutex mu;
+    static std::vector<std::unique_ptr<qkg::Workspace>> ws;
+    int dev = 0;
+    QKG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)ws.size() <= dev) ws.resize(dev + 1);
+    if (!ws[dev]) ws[dev] = std::make_unique<qkg::Workspace>();
+    return *ws[dev];
 }
 
 void fill_result(qkrylov_lanczos_result_f64_t* r, const qkg::LanczosOut& o) {
@@ -332,6 +345,29 @@ int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* dx
         H.to_internal_f32(x, h->x32.as<float2>(), s);
         H.apply_f32(h->x32.as<float2>(), h->y32.as<float2>(), s);
         H.to_reference_f32(h->y32.as<float2>(), y, s);
+    });
+}
+
+int qkrylov_vector_dot_device_f64(const void* dx, const void* dy, uint64_t n, double* result, void* stream) {
+    if (!result || (n && (!dx || !dy))) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        result[0] = result[1] = 0.0;
+        if (!n) return;
+        const auto v = qkg::dot_f64(static_cast<const double2*>(dx), static_cast<const double2*>(dy), n,
+                                    device_workspace(), static_cast<cudaStream_t>(stream));
+        result[0] = v.real();
+        result[1] = v.imag();
+    });
+}
+int qkrylov_vector_dot_device_f32(const void* dx, const void* dy, uint64_t n, double* result, void* stream) {
+    if (!result || (n && (!dx || !dy))) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        result[0] = result[1] = 0.0;
+        if (!n) return;
+        const auto v = qkg::dot_f32(static_cast<const float2*>(dx), static_cast<const float2*>(dy), n,
+                                    device_workspace(), static_cast<cudaStream_t>(stream));
+        result[0] = v.real();
+        result[1] = v.imag();
     });
 }
 
