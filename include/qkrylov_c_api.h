@@ -177,6 +177,20 @@ int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* d_
 int qkrylov_vector_dot_device_f64(const void* d_x, const void* d_y, uint64_t n, double* result, void* stream);
 int qkrylov_vector_dot_device_f32(const void* d_x, const void* d_y, uint64_t n, double* result, void* stream);
 
+/* Same result as qkrylov_vector_dot_device_f64, but the library allocates
+ * nothing: no counterpart in the reference.  It is for callers that cannot let
+ * a library call cudaMalloc -- applications that reserve the GPU's memory in
+ * their own pool or run under a hard memory cap, and latency-critical loops
+ * that cannot take cudaMalloc's implicit device synchronisation.  The partial
+ * sums go to a fixed 256 KiB array compiled into the library (held by every
+ * GPU that loads it until exit), so n is limited to 134,217,728 complex
+ * elements; larger n returns QKRYLOV_ERROR_INVALID_ARG.  All calls share that
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  The first call on a GPU looks up the array's address there and
+ * should come before any stream capture. */
+int qkrylov_vector_dot_device_f64_noalloc(const void* d_x, const void* d_y, uint64_t n, double* result,
+                                          void* stream);
+
 /* Lanczos ground state, FP64 (reference semantics: full reorthogonalisation,
  * stop when |E_k - E_{k-1}| < tol; lanczos.cpp:101-202).  The start vector is
  * the reference's (mt19937(1234), uniform[-1,1] complex) unless v0 (dim complex,

@@ -105,6 +105,7 @@ _SIGS = {
     "qkrylov_kernel_launches": (_u64, []),
     "qkrylov_vector_dot_device_f64": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_vector_dot_device_f32": (_i, [_vp, _vp, _u64, _dp, _vp]),
+    "qkrylov_vector_dot_device_f64_noalloc": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_set_device": (_i, [_i]),
     "qkrylov_device_synchronize": (_i, []),
     "qkrylov_davidson_lowest_complex_f64": (_i, [_vp, _i, _i, _d, _dp, _dp, _c.POINTER(DavidsonResultC)]),
