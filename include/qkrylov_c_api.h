@@ -268,9 +268,12 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* n_outer, int* n_inner
                              int* diag_mode);
 
 /* SpMV kernel choice: generic = 0 lets the library use its table-driven fast
- * kernel when the Hamiltonian qualifies (32-bit states, coded diagonal);
- * generic = 1 forces the generic kernel.  *fast_in_use (optional) reports the
- * kernel that applies from now on. */
+ * kernel when the Hamiltonian qualifies (32-bit states, coded diagonal), in
+ * the variant its autotuner measured fastest at creation; generic = 1 forces
+ * the generic kernel; 2 the fast kernel with one row per thread; 3 the fast
+ * kernel with shared-memory staging of each outer block's slice of x (when a
+ * block fits); 4 the fast kernel with four rows per thread.  *fast_in_use
+ * (optional) reports whether the fast kernel applies. */
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use);
 
 /* Time `reps` back-to-back applies of the FP32 (fp32 != 0) or FP64 kernel on

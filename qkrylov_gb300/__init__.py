@@ -351,11 +351,14 @@ class MatrixFreeHamiltonian(_Handle):
         _check(lib().qkrylov_hamiltonian_info(self._h, *[_c.byref(x) for x in v]))
         return dict(zip(["n_outer", "n_inner", "n_mixed", "n_diag", "diag_mode"], [x.value for x in v]))
 
-    def select_kernel(self, generic=False):
-        """Force the generic SpMV kernel (True) or allow the fast one (False);
-        returns whether the fast kernel is in use."""
+    def select_kernel(self, generic=False, mode=None):
+        """Force the generic SpMV kernel (True) or allow the fast one (False).
+        mode picks a kernel directly: 0 autotuned, 1 generic, 2 fast with one
+        row per thread, 3 fast with shared-memory staging, 4 fast with four
+        rows per thread.  Returns whether the fast kernel is in use."""
+        m = int(mode) if mode is not None else int(bool(generic))
         f = _c.c_int()
-        _check(lib().qkrylov_hamiltonian_select_kernel(self._h, int(bool(generic)), _c.byref(f)))
+        _check(lib().qkrylov_hamiltonian_select_kernel(self._h, m, _c.byref(f)))
         return bool(f.value)
 
     def benchmark_apply(self, fp32=True, reps=10):

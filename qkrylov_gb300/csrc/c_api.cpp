@@ -382,8 +382,8 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* no, int* ni, int* nm,
 }
 
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use) {
-    if (!h || !h->ptr) return QKRYLOV_ERROR_INVALID_ARG;
-    h->ptr->force_generic(generic != 0);
+    if (!h || !h->ptr || generic < 0 || generic > 4) return QKRYLOV_ERROR_INVALID_ARG;
+    h->ptr->set_kernel_mode(generic);
     if (fast_in_use) *fast_in_use = h->ptr->fast() ? 1 : 0;
     return QKRYLOV_SUCCESS;
 }

@@ -29,6 +29,20 @@ struct DBuf {
 
 enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
 
+// Fast SpMV kernel variants: one row per thread, the outer block's slice of x
+// staged in shared memory, four rows per thread.
+enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2 };
+
+// Device-resident Lanczos step: the SpMV reads its vectors through a device
+// pointer table indexed by a device step counter (x = vtab[k], y = vtab[k+1]),
+// scales y by sig[k] and writes one Re<x, y> partial per block to apart.
+struct LanczosHooks {
+    const void* const* vtab = nullptr;
+    const int* kstep = nullptr;
+    const double* sig = nullptr;
+    double2* apart = nullptr;
+};
+
 // Per-precision copy of the compiled term lists.
 struct TermSet {
     DBuf outer, inner, mixed, diag, all, vars;
@@ -51,6 +65,9 @@ public:
     // y = H x on device vectors in internal order (interleaved complex).
     void apply_f64(const double2* x, double2* y, cudaStream_t s) const;
     void apply_f32(const float2* x, float2* y, cudaStream_t s) const;
+    // One FP32 SpMV of the device-resident Lanczos step (fast kernel only);
+    // writes n_items() partials to lz.apart.
+    void apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) const;
 
     // Diagonal H_ii (complex, internal order) into a device buffer.
     void diagonal_f64(double2* d, cudaStream_t s) const;
@@ -77,8 +94,26 @@ public:
     int diag_mode() const { return diag_mode_; }
     size_t n_items() const { return n_items_; }
     bool fast() const { return fast_ && !force_generic_; }
-    void force_generic(bool on) { force_generic_ = on; }
+    // kernel mode: 0 automatic (autotuned), 1 generic kernel, 2 fast kernel
+    // one row per thread, 3 fast kernel with shared-memory staging, 4 fast
+    // kernel four rows per thread
+    void set_kernel_mode(int m) { mode_ = m; force_generic_ = (m == 1); }
+    void force_generic(bool on) { set_kernel_mode(on ? 1 : 0); }
+    // fast-kernel variant for vectors of elem_bytes per element
+    FastVariant variant(size_t elem_bytes) const {
+        const bool can_stage = max_block_ > 0 && max_block_ * elem_bytes <= kStageLimit;
+        if (mode_ == 2) return FV_ROW;
+        if (mode_ == 3) return can_stage ? FV_STAGED : FV_ROW;
+        if (mode_ == 4) return FV_ROWS4;
+        const FastVariant v = pref_[elem_bytes == 16 ? 1 : 0];
+        return (v == FV_STAGED && !can_stage) ? FV_ROW : v;
+    }
+    bool staged(size_t elem_bytes) const { return fast() && variant(elem_bytes) == FV_STAGED; }
+    // autotuner record: mean ms of [precision][variant] (0 when not measured)
+    double tuned_ms(int prec, int v) const { return tune_ms_[prec][v]; }
     size_t inner_table_entries() const { return n_ient_; }
+    size_t lanczos_parts() const;  // partial sums written by apply_lanczos_f32
+    static constexpr size_t kStageLimit = 200 * 1024;
 
 private:
     void build_diagonal();
@@ -90,7 +125,13 @@ private:
         DBuf outer, inner, mixed, vars;
         int n_outer = 0, n_inner = 0, n_mixed = 0, outer_has_j = 0;
     };
+    void autotune();
     bool fast_ = false, force_generic_ = false, unif_ = false;
+    int mode_ = 0;
+    FastVariant pref_[2] = {FV_ROWS4, FV_ROWS4};
+    double tune_ms_[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    DBuf items_blk_;            // one work item per outer block (staged kernel)
+    size_t n_items_blk_ = 0, max_block_ = 0;
     double u_ar_ = 0.0, u_ai_ = 0.0;
     int rbits_ = 0;
     size_t n_ient_ = 0;

@@ -49,6 +49,7 @@ constexpr int kBlock = 256;
 constexpr uint32_t kChunk = 1024;
 constexpr int kMaxOuter = 256;
 constexpr int kMaxInnerTable = 512;  // inner terms a table may reference
+constexpr uint32_t kEllEmpty = 0xFFFFFFFFu;
 constexpr size_t kSmemTermBudget = 40 * 1024;
 
 template <class S, class A>
@@ -341,9 +342,40 @@ struct FastParams {
     const KVar<A>* vars;
     int n_mixed;
     int diag_mode;
+    int n_dtab;
     const void* dcode;
     const A* dtab;
+    // Lanczos mode (all null otherwise): x = vtab[*kstep], y = vtab[*kstep + 1],
+    // y is scaled by sig[*kstep], and each block writes Re sum conj(x) y to apart.
+    const void* const* vtab;
+    const int* kstep;
+    const double* sig;
+    double2* apart;
 };
+
+// Compensated accumulation of a*b into (hi, lo) (TwoProduct + TwoSum).
+__device__ __forceinline__ void ffma_acc(float& hi, float& lo, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float t = hi + p;
+    const float z = t - hi;
+    lo += ((hi - (t - z)) + (p - z)) + e;
+    hi = t;
+}
+__device__ __forceinline__ void ffma_acc(double& hi, double& lo, double a, double b) { hi = fma(a, b, hi); }
+
+__device__ __forceinline__ double block_sum_d(double v) {
+    __shared__ double sh[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : 0.0;
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
 
 __device__ __forceinline__ bool in_basis_fast(int ng, uint32_t g0, uint32_t g1, int p0, int p1, int no_double, int N,
                                               uint32_t s) {
@@ -353,15 +385,40 @@ __device__ __forceinline__ bool in_basis_fast(int ng, uint32_t g0, uint32_t g1, 
     return true;
 }
 
-template <class T, class A, bool REAL, bool UNIF>
-__global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x,
-                                                           typename V2<T>::t* __restrict__ y) {
+constexpr int kMaxMixedSmem = 64;
+// STAGE: the work item is a whole outer block and its x slice is staged in
+// shared memory, so inner-table gathers read shared memory.
+template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE>
+__global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
+                                                           typename V2<T>::t* __restrict__ y_in) {
     using T2 = typename V2<T>::t;
+    extern __shared__ __align__(16) unsigned char fast_smem[];
+    T2* xs = reinterpret_cast<T2*>(fast_smem);
+    const T2* __restrict__ x = x_in;
+    T2* __restrict__ y = y_in;
+    A scale = (A)1;
+    if (p.vtab) {
+        const int k = *p.kstep;
+        x = static_cast<const T2*>(p.vtab[k]);
+        y = static_cast<T2*>(const_cast<void*>(p.vtab[k + 1]));
+        scale = (A)p.sig[k];
+    }
+    A dot_hi = 0, dot_lo = 0;  // Re sum conj(x) y over this thread's rows (Lanczos mode)
     __shared__ OutEnt<A> s_out[kMaxOuter];
     __shared__ A s_iamp[2 * kMaxInnerTable];
+    __shared__ KTerm<uint32_t, A> s_mixed[kMaxMixedSmem];
+    __shared__ A s_dtab[512];
     __shared__ int s_n;
+    const bool mixed_smem = p.n_mixed <= kMaxMixedSmem;
+    if (mixed_smem)
+        for (int t = threadIdx.x; t < p.n_mixed; t += blockDim.x) s_mixed[t] = p.mixed[t];
+    if (p.diag_mode == DIAG_U8)  // at most 256 values
+        for (int t = threadIdx.x; t < 2 * p.n_dtab; t += blockDim.x) s_dtab[t] = p.dtab[t];
+    const KTerm<uint32_t, A>* mixed = mixed_smem ? s_mixed : p.mixed;
     const WorkItem it = p.items[blockIdx.x];
     const uint32_t block_off = __ldg(p.outer_off + it.a);
+    if (STAGE)  // the item is the whole block: rows [block_off, block_off + count)
+        for (uint32_t i = threadIdx.x; i < it.count; i += blockDim.x) xs[i] = x[block_off + i];
     if (!UNIF) {
         // inner-term amplitudes with the sign their JW mask takes on this block's outer bits
         const uint32_t sa = it.a << p.n_in;
@@ -402,47 +459,49 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
     }
     __syncthreads();
     const int nout = s_n;
+    const uint32_t rmask = (1u << p.rbits) - 1u;
     for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
         const uint32_t row = (uint32_t)it.row0 + r;
         const uint32_t pidx = it.inner_base + r;
         const uint32_t b = p.inner_state ? __ldg(p.inner_state + pidx) : pidx;
         const uint32_t s = (it.a << p.n_in) | b;
-        A accr, acci;
-        {
-            const uint32_t c = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
-                                                      : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
-            const A dr = __ldg(p.dtab + 2 * c);
-            const T2 xv = x[row];
-            accr = dr * (A)xv.x;
-            acci = dr * (A)xv.y;
-            if (!REAL) {
-                const A di = __ldg(p.dtab + 2 * c + 1);
-                accr = fma(-di, (A)xv.y, accr);
-                acci = fma(di, (A)xv.x, acci);
-            }
-        }
+        // ELL group of this row (32 rows per group, lane = r % 32)
+        const uint32_t grp = it.pad + (r >> 5);
+        const uint32_t e0 = __ldg(p.iptr + grp) + (r & 31u), e1 = __ldg(p.iptr + grp + 1);
+        const uint32_t dc = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
+                                                   : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
+        const T2 xd = STAGE ? xs[r] : x[row];
+        A accr = 0, acci = 0;
+#pragma unroll 2
         for (int k = 0; k < nout; ++k) {
             const OutEnt<A> e = s_out[k];
             const T2 xv = x[row + e.delta];
-            const A sg = (__popc(s & e.J) & 1) ? (A)-1 : (A)1;
-            cmac<A>(accr, acci, sg * e.ar, sg * e.ai, xv, REAL);
+            A ar = e.ar, ai = e.ai;
+            if (OJ && (__popc(s & e.J) & 1)) {
+                ar = -ar;
+                ai = -ai;
+            }
+            cmac<A>(accr, acci, ar, ai, xv, REAL);
         }
-        const uint32_t e0 = __ldg(p.iptr + pidx), e1 = __ldg(p.iptr + pidx + 1);
-        const uint32_t rmask = (1u << p.rbits) - 1u;
-#pragma unroll 4
-        for (uint32_t e = e0; e < e1; ++e) {
+#pragma unroll 2
+        for (uint32_t e = e0; e < e1; e += 32) {
             const uint32_t ent = __ldg(p.ient + e);
-            const T2 xv = x[block_off + (ent & rmask)];
+            if (ent == kEllEmpty) break;  // a row's entries fill its first slots
+            const T2 xv = STAGE ? xs[ent & rmask] : x[block_off + (ent & rmask)];
             if (UNIF) {
                 cmac<A>(accr, acci, p.u_ar, p.u_ai, xv, REAL);
             } else {
                 const uint32_t t = ent >> (p.rbits + 1);
-                const A sg = ((ent >> p.rbits) & 1u) ? (A)-1 : (A)1;
-                cmac<A>(accr, acci, sg * s_iamp[2 * t], sg * s_iamp[2 * t + 1], xv, REAL);
+                A ar = s_iamp[2 * t], ai = s_iamp[2 * t + 1];
+                if ((ent >> p.rbits) & 1u) {
+                    ar = -ar;
+                    ai = -ai;
+                }
+                cmac<A>(accr, acci, ar, ai, xv, REAL);
             }
         }
         for (int k = 0; k < p.n_mixed; ++k) {
-            const KTerm<uint32_t, A> t = p.mixed[k];
+            const KTerm<uint32_t, A> t = mixed[k];
             if ((s & t.C) != t.V) continue;
             const uint32_t s2 = s ^ t.X;
             if ((t.flags & 1u) && !in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2))
@@ -453,10 +512,225 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
             term_amp<uint32_t, A>(t, s, p.vars, ar, ai);
             cmac<A>(accr, acci, ar, ai, x[idx], REAL);
         }
+        {
+            const A dr = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc] : __ldg(p.dtab + 2 * dc);
+            accr = fma(dr, (A)xd.x, accr);
+            acci = fma(dr, (A)xd.y, acci);
+            if (!REAL) {
+                const A di = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc + 1] : __ldg(p.dtab + 2 * dc + 1);
+                accr = fma(-di, (A)xd.y, accr);
+                acci = fma(di, (A)xd.x, acci);
+            }
+        }
         T2 out;
-        out.x = (T)accr;
-        out.y = (T)acci;
+        out.x = (T)(accr * scale);
+        out.y = (T)(acci * scale);
         y[row] = out;
+        if (p.apart) {
+            ffma_acc(dot_hi, dot_lo, (A)xd.x, (A)out.x);
+            ffma_acc(dot_hi, dot_lo, (A)xd.y, (A)out.y);
+        }
+    }
+    if (p.apart) {
+        const double s = block_sum_d((double)dot_hi + (double)dot_lo);
+        if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2(s, 0.0);
+    }
+}
+
+// Unstaged fast kernel, four rows per thread: a 1024-row work item gives
+// thread t the rows t, t+256, t+512, t+768.  Every outer entry and every
+// straddling term is read once per thread and applied to its four rows, which
+// also gives four independent gathers in flight per entry; the four rows'
+// ELL walks advance together.
+constexpr int kRowsPerThread = 4;
+static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread rows per thread");
+
+template <class T, class A, bool REAL, bool UNIF, bool OJ>
+__global__ void __launch_bounds__(kBlock) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
+                                                           typename V2<T>::t* __restrict__ y_in) {
+    using T2 = typename V2<T>::t;
+    constexpr int RT = kRowsPerThread;
+    const T2* __restrict__ x = x_in;
+    T2* __restrict__ y = y_in;
+    A scale = (A)1;
+    if (p.vtab) {
+        const int k = *p.kstep;
+        x = static_cast<const T2*>(p.vtab[k]);
+        y = static_cast<T2*>(const_cast<void*>(p.vtab[k + 1]));
+        scale = (A)p.sig[k];
+    }
+    __shared__ OutEnt<A> s_out[kMaxOuter];
+    __shared__ A s_iamp[2 * kMaxInnerTable];
+    __shared__ KTerm<uint32_t, A> s_mixed[kMaxMixedSmem];
+    __shared__ A s_dtab[512];
+    __shared__ int s_n;
+    const bool mixed_smem = p.n_mixed <= kMaxMixedSmem;
+    if (mixed_smem)
+        for (int t = threadIdx.x; t < p.n_mixed; t += blockDim.x) s_mixed[t] = p.mixed[t];
+    if (p.diag_mode == DIAG_U8)
+        for (int t = threadIdx.x; t < 2 * p.n_dtab; t += blockDim.x) s_dtab[t] = p.dtab[t];
+    const KTerm<uint32_t, A>* mixed = mixed_smem ? s_mixed : p.mixed;
+    const WorkItem it = p.items[blockIdx.x];
+    const uint32_t block_off = __ldg(p.outer_off + it.a);
+    if (!UNIF) {
+        const uint32_t sa = it.a << p.n_in;
+        for (int t = threadIdx.x; t < p.n_inner; t += blockDim.x) {
+            const KTerm<uint32_t, A> k = p.inner[t];
+            const bool neg = __popc(sa & k.J) & 1;
+            s_iamp[2 * t] = neg ? -k.ar : k.ar;
+            s_iamp[2 * t + 1] = neg ? -k.ai : k.ai;
+        }
+    }
+    if (threadIdx.x < 32) {
+        const uint32_t b0 = p.inner_state ? __ldg(p.inner_state + it.inner_base) : it.inner_base;
+        const uint32_t s0 = (it.a << p.n_in) | b0;
+        int base = 0;
+        for (int t0 = 0; t0 < p.n_outer; t0 += 32) {
+            const int ti = t0 + (int)threadIdx.x;
+            bool ok = false;
+            OutEnt<A> e;
+            if (ti < p.n_outer) {
+                const KTerm<uint32_t, A> t = p.outer[ti];
+                if ((s0 & t.C) == t.V) {
+                    const uint32_t s2 = s0 ^ t.X;
+                    if (!(t.flags & 1u) || in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2)) {
+                        ok = true;
+                        e.delta = (int32_t)(__ldg(p.outer_off + (s2 >> p.n_in)) - block_off);
+                        e.J = t.J;
+                        e.ar = t.ar;
+                        e.ai = t.ai;
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) s_out[base + __popc(m & ((1u << threadIdx.x) - 1u))] = e;
+            base += __popc(m);
+        }
+        if (threadIdx.x == 0) s_n = base;
+    }
+    __syncthreads();
+    const int nout = s_n;
+    const uint32_t rmask = (1u << p.rbits) - 1u;
+
+    uint32_t s[RT], e0[RT], e1[RT];
+    A ar_[RT], ai_[RT];
+    bool live[RT];
+    const T2* xr = x + (uint32_t)it.row0 + threadIdx.x;  // row q of this thread is xr[q * kBlock]
+#pragma unroll
+    for (int q = 0; q < RT; ++q) {
+        const uint32_t r = threadIdx.x + q * kBlock;
+        live[q] = r < it.count;
+        const uint32_t rr = live[q] ? r : 0;
+        const uint32_t pidx = it.inner_base + rr;
+        const uint32_t b = p.inner_state ? __ldg(p.inner_state + pidx) : pidx;
+        s[q] = (it.a << p.n_in) | b;
+        const uint32_t grp = it.pad + (rr >> 5);
+        e0[q] = __ldg(p.iptr + grp) + (rr & 31u);
+        e1[q] = live[q] ? __ldg(p.iptr + grp + 1) : 0u;
+        ar_[q] = 0;
+        ai_[q] = 0;
+    }
+    for (int k = 0; k < nout; ++k) {
+        const OutEnt<A> e = s_out[k];
+        T2 xv[RT];
+#pragma unroll
+        for (int q = 0; q < RT; ++q)
+            if (live[q]) xv[q] = xr[q * kBlock + e.delta];
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            if (!live[q]) continue;
+            A cr = e.ar, ci = e.ai;
+            if (OJ && (__popc(s[q] & e.J) & 1)) {
+                cr = -cr;
+                ci = -ci;
+            }
+            cmac<A>(ar_[q], ai_[q], cr, ci, xv[q], REAL);
+        }
+    }
+    // the four rows' ELL walks, slot by slot
+    bool more = true;
+    while (more) {
+        more = false;
+        uint32_t ent[RT];
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            ent[q] = kEllEmpty;
+            if (e0[q] < e1[q]) ent[q] = __ldg(p.ient + e0[q]);
+        }
+        T2 xv[RT];
+#pragma unroll
+        for (int q = 0; q < RT; ++q)
+            if (ent[q] != kEllEmpty) xv[q] = x[block_off + (ent[q] & rmask)];
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            if (ent[q] == kEllEmpty) {
+                e0[q] = e1[q];
+                continue;
+            }
+            if (UNIF) {
+                cmac<A>(ar_[q], ai_[q], p.u_ar, p.u_ai, xv[q], REAL);
+            } else {
+                const uint32_t t = ent[q] >> (p.rbits + 1);
+                A cr = s_iamp[2 * t], ci = s_iamp[2 * t + 1];
+                if ((ent[q] >> p.rbits) & 1u) {
+                    cr = -cr;
+                    ci = -ci;
+                }
+                cmac<A>(ar_[q], ai_[q], cr, ci, xv[q], REAL);
+            }
+            e0[q] += 32;
+            more = more || (e0[q] < e1[q]);
+        }
+    }
+    for (int k = 0; k < p.n_mixed; ++k) {
+        const uint32_t C = mixed[k].C, V = mixed[k].V;
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            if (!live[q] || (s[q] & C) != V) continue;
+            const KTerm<uint32_t, A> t = mixed[k];
+            const uint32_t s2 = s[q] ^ t.X;
+            if ((t.flags & 1u) && !in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2))
+                continue;
+            const uint32_t b2 = s2 & p.in_mask;
+            const uint32_t idx = __ldg(p.outer_off + (s2 >> p.n_in)) + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+            A cr, ci;
+            term_amp<uint32_t, A>(t, s[q], p.vars, cr, ci);
+            cmac<A>(ar_[q], ai_[q], cr, ci, x[idx], REAL);
+        }
+    }
+    A dot_hi = 0, dot_lo = 0;
+    T2 xd[RT];
+    uint32_t dc[RT];
+#pragma unroll
+    for (int q = 0; q < RT; ++q) {
+        const uint32_t row = (uint32_t)it.row0 + (live[q] ? threadIdx.x + q * kBlock : 0u);
+        dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
+                                       : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
+        xd[q] = x[row];
+    }
+#pragma unroll
+    for (int q = 0; q < RT; ++q) {
+        if (!live[q]) continue;
+        const A dr = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc[q]] : __ldg(p.dtab + 2 * dc[q]);
+        A accr = fma(dr, (A)xd[q].x, ar_[q]);
+        A acci = fma(dr, (A)xd[q].y, ai_[q]);
+        if (!REAL) {
+            const A di = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc[q] + 1] : __ldg(p.dtab + 2 * dc[q] + 1);
+            accr = fma(-di, (A)xd[q].y, accr);
+            acci = fma(di, (A)xd[q].x, acci);
+        }
+        T2 out;
+        out.x = (T)(accr * scale);
+        out.y = (T)(acci * scale);
+        y[(uint32_t)it.row0 + threadIdx.x + q * kBlock] = out;
+        if (p.apart) {
+            ffma_acc(dot_hi, dot_lo, (A)xd[q].x, (A)out.x);
+            ffma_acc(dot_hi, dot_lo, (A)xd[q].y, (A)out.y);
+        }
+    }
+    if (p.apart) {
+        const double sum = block_sum_d((double)dot_hi + (double)dot_lo);
+        if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2(sum, 0.0);
     }
 }
 
@@ -658,6 +932,9 @@ void pack(const std::vector<const HostTerm*>& lst, std::vector<KTerm<S, A>>& out
 }
 }  // namespace
 
+template <class T, class A>
+static void allow_stage_smem(size_t bytes);
+
 void Hamiltonian::build_fast() {
     const Basis& B = *basis_;
     fast_ = false;
@@ -681,15 +958,13 @@ void Hamiltonian::build_fast() {
     rbits_ = std::max(1, B.n_in);
     const int tbits = 32 - rbits_ - 1;
     if (tbits < 1 || (inner.size() > (1ull << tbits))) return;
-    std::vector<uint32_t> ptr(P + 1, 0), ent;
     unif_ = true;
     const std::complex<double> amp0 = inner.empty() ? std::complex<double>(0.0) : inner[0]->amp;
     for (const HostTerm* h : inner)
         if (h->amp != amp0 || (h->J != 0)) unif_ = false;
-    for (uint32_t pi = 0; pi < P; ++pi) {
-        ptr[pi] = (uint32_t)ent.size();
-        const uint32_t b = B.inner_all ? pi : B.inner_state[pi];
-        if (!B.inner_all && !present[__builtin_popcount(b)]) continue;
+    // Entries of one inner configuration, in term order.
+    auto row_entries = [&](uint32_t b, std::vector<uint32_t>& out) {
+        out.clear();
         for (size_t t = 0; t < inner.size(); ++t) {
             const HostTerm& h = *inner[t];
             if ((b & h.C) != h.V) continue;
@@ -698,14 +973,53 @@ void Hamiltonian::build_fast() {
             if (h.check && !B.inner_all && __builtin_popcount(b2) != __builtin_popcount(b)) continue;
             const uint32_t r2 = B.inner_all ? b2 : B.inner_rank[b2];
             const uint32_t sg = __builtin_popcountll((uint64_t)b & h.J & inm) & 1u;
-            ent.push_back(r2 | (sg << rbits_) | ((uint32_t)t << (rbits_ + 1)));
+            out.push_back(r2 | (sg << rbits_) | ((uint32_t)t << (rbits_ + 1)));
         }
-        if (ent.size() > (1ull << 30)) return;
+    };
+    // Warp-aligned ELL layout: the rows of a class are grouped by 32 (a work
+    // item starts at a multiple of 32 inside its class, so lane = row % 32);
+    // group g holds W_g slots per row, slot j of the 32 rows stored
+    // contiguously, unused slots = kEllEmpty.  gptr[g] is the group's first slot.
+    std::vector<uint32_t> gptr(1, 0), ent, class_gbase(B.n_in + 2, 0), rowbuf;
+    std::vector<std::vector<uint32_t>> grp(32);
+    const int nclass = B.inner_all ? 1 : B.n_in + 1;
+    for (int m = 0; m < nclass; ++m) {
+        class_gbase[m] = (uint32_t)(gptr.size() - 1);
+        const uint32_t cbase = B.inner_all ? 0u : B.class_base[m];
+        const uint32_t csize = B.inner_all ? P : (uint32_t)(B.class_base[m + 1] - B.class_base[m]);
+        const bool use = B.inner_all || present[m];
+        for (uint32_t g0 = 0; g0 < csize; g0 += 32) {
+            size_t w = 0;
+            for (uint32_t l = 0; l < 32; ++l) {
+                grp[l].clear();
+                if (use && g0 + l < csize) {
+                    const uint32_t pi = cbase + g0 + l;
+                    row_entries(B.inner_all ? pi : B.inner_state[pi], grp[l]);
+                }
+                w = std::max(w, grp[l].size());
+            }
+            for (size_t j = 0; j < w; ++j)
+                for (uint32_t l = 0; l < 32; ++l) ent.push_back(j < grp[l].size() ? grp[l][j] : kEllEmpty);
+            gptr.push_back((uint32_t)ent.size());
+            if (ent.size() > (1ull << 31)) return;
+        }
     }
-    ptr[P] = (uint32_t)ent.size();
     n_ient_ = ent.size();
-    upload_vec(iptr_, ptr);
+    upload_vec(iptr_, gptr);
     upload_vec(ient_, ent);
+    // each work item records the ELL group of its first row
+    auto set_groups = [&](std::vector<WorkItem>& items) {
+        for (auto& w : items) {
+            const int m = B.inner_all ? 0 : B.inner_class_of(w.a);
+            const uint32_t r_loc = w.inner_base - (B.inner_all ? 0u : B.class_base[m]);
+            w.pad = class_gbase[m] + r_loc / 32;
+        }
+    };
+    {
+        auto items = B.work_items(kChunk);
+        set_groups(items);
+        upload_vec(items_, items);
+    }
     u_ar_ = amp0.real();
     u_ai_ = amp0.imag();
     auto build = [&](auto tag, FastSet& fs) {
@@ -727,7 +1041,57 @@ void Hamiltonian::build_fast() {
     };
     build(double(), f64s_);
     build(float(), f32s_);
+    // one item per outer block for the staged kernel
+    auto bitems = B.work_items(0xFFFFFFFFu);
+    set_groups(bitems);
+    max_block_ = 0;
+    for (const auto& w : bitems) max_block_ = std::max<size_t>(max_block_, w.count);
+    n_items_blk_ = bitems.size();
+    upload_vec(items_blk_, bitems);
+    if (max_block_ * 8 <= kStageLimit) allow_stage_smem<float, float>(std::max<size_t>(max_block_ * 8, 1));
+    if (max_block_ * 16 <= kStageLimit) allow_stage_smem<double, double>(std::max<size_t>(max_block_ * 16, 1));
     fast_ = true;
+    autotune();
+}
+
+// Autotuner: for sectors large enough to matter, time each fast-kernel
+// variant per precision and keep the fastest for mode 0.
+void Hamiltonian::autotune() {
+    const uint64_t n = dim();
+    if (n < (1ull << 20)) return;  // small sectors: four rows per thread
+    const int saved = mode_;
+    for (int prec = 0; prec < 2; ++prec) {
+        const size_t e = prec ? sizeof(double2) : sizeof(float2);
+        DBuf x(n * e), y(n * e);
+        QKG_CUDA(cudaMemsetAsync(x.p, 0, n * e, stream_));
+        cudaEvent_t a, b;
+        QKG_CUDA(cudaEventCreate(&a));
+        QKG_CUDA(cudaEventCreate(&b));
+        double best = 0.0;
+        for (int v = 0; v < 3; ++v) {
+            if (v == FV_STAGED && !(max_block_ * e <= kStageLimit)) continue;
+            mode_ = v == FV_ROW ? 2 : v == FV_STAGED ? 3 : 4;
+            auto run = [&] {
+                if (prec) apply_f64(x.as<double2>(), y.as<double2>(), stream_);
+                else apply_f32(x.as<float2>(), y.as<float2>(), stream_);
+            };
+            run();
+            QKG_CUDA(cudaEventRecord(a, stream_));
+            for (int r = 0; r < 3; ++r) run();
+            QKG_CUDA(cudaEventRecord(b, stream_));
+            QKG_CUDA(cudaEventSynchronize(b));
+            float ms = 0.f;
+            QKG_CUDA(cudaEventElapsedTime(&ms, a, b));
+            tune_ms_[prec][v] = ms / 3.0;
+            if (best == 0.0 || tune_ms_[prec][v] < best) {
+                best = tune_ms_[prec][v];
+                pref_[prec] = (FastVariant)v;
+            }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    mode_ = saved;
 }
 
 template <class T, class A>
@@ -735,9 +1099,14 @@ static void launch_fast(const DevBasis& b, const DBuf& items, size_t n_items, co
                         int rbits, bool unif, double uar, double uai, const DBuf& outer, int n_outer, int outer_has_j,
                         const DBuf& inner, int n_inner, const DBuf& mixed, const DBuf& vars, int n_mixed, bool real,
                         int diag_mode, const DBuf& dcode, const DBuf& dtab, const typename V2<T>::t* x,
-                        typename V2<T>::t* y, cudaStream_t s) {
+                        typename V2<T>::t* y, cudaStream_t s, FastVariant var, size_t stage_smem,
+                        const LanczosHooks* lz = nullptr) {
     if (!n_items) return;
     FastParams<A> p;
+    p.vtab = lz ? lz->vtab : nullptr;
+    p.kstep = lz ? lz->kstep : nullptr;
+    p.sig = lz ? lz->sig : nullptr;
+    p.apart = lz ? lz->apart : nullptr;
     p.n_in = b.n_in;
     p.in_mask = (uint32_t)b.in_mask;
     p.ngroups = b.ngroups;
@@ -765,17 +1134,59 @@ static void launch_fast(const DevBasis& b, const DBuf& items, size_t n_items, co
     p.vars = vars.as<KVar<A>>();
     p.n_mixed = n_mixed;
     p.diag_mode = diag_mode;
+    p.n_dtab = (int)(dtab.bytes / (2 * sizeof(A)));
     p.dcode = dcode.p;
     p.dtab = dtab.as<A>();
     const unsigned g = (unsigned)n_items;
-    if (real) {
-        if (unif) spmv_fast_kernel<T, A, true, true><<<g, kBlock, 0, s>>>(p, x, y);
-        else spmv_fast_kernel<T, A, true, false><<<g, kBlock, 0, s>>>(p, x, y);
-    } else {
-        if (unif) spmv_fast_kernel<T, A, false, true><<<g, kBlock, 0, s>>>(p, x, y);
-        else spmv_fast_kernel<T, A, false, false><<<g, kBlock, 0, s>>>(p, x, y);
+    const int key = (var == FV_STAGED ? 8 : 0) | (real ? 4 : 0) | (unif ? 2 : 0) | (outer_has_j ? 1 : 0);
+    const size_t sm = stage_smem;
+    if (var == FV_ROWS4) {
+        switch (key) {
+            case 0: spmv_rows_kernel<T, A, false, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 1: spmv_rows_kernel<T, A, false, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 2: spmv_rows_kernel<T, A, false, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 3: spmv_rows_kernel<T, A, false, true, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 4: spmv_rows_kernel<T, A, true, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 5: spmv_rows_kernel<T, A, true, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 6: spmv_rows_kernel<T, A, true, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            default: spmv_rows_kernel<T, A, true, true, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+        }
+        QKG_LAUNCHED();
+        return;
+    }
+    switch (key) {
+        case 0: spmv_fast_kernel<T, A, false, false, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 1: spmv_fast_kernel<T, A, false, false, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 2: spmv_fast_kernel<T, A, false, true, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 3: spmv_fast_kernel<T, A, false, true, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 4: spmv_fast_kernel<T, A, true, false, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 5: spmv_fast_kernel<T, A, true, false, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 6: spmv_fast_kernel<T, A, true, true, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 7: spmv_fast_kernel<T, A, true, true, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+        case 8: spmv_fast_kernel<T, A, false, false, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        case 9: spmv_fast_kernel<T, A, false, false, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        case 10: spmv_fast_kernel<T, A, false, true, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        case 11: spmv_fast_kernel<T, A, false, true, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        case 12: spmv_fast_kernel<T, A, true, false, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        case 13: spmv_fast_kernel<T, A, true, false, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        case 14: spmv_fast_kernel<T, A, true, true, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+        default: spmv_fast_kernel<T, A, true, true, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
     }
     QKG_LAUNCHED();
+}
+
+// Staged variants may need more than 48 KB of dynamic shared memory.
+template <class T, class A>
+static void allow_stage_smem(size_t bytes) {
+    const int b = (int)bytes;
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
 }
 
 Hamiltonian::~Hamiltonian() {
@@ -891,9 +1302,12 @@ static void launch_spmv(const DevBasis& b, const TermSet& ts, const DBuf& items,
 
 void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const {
     if (fast()) {
-        launch_fast<double, double>(*db_, items_, n_items_, iptr_, ient_, rbits_, unif_, u_ar_, u_ai_, f64s_.outer,
-                                    f64s_.n_outer, f64s_.outer_has_j, f64s_.inner, f64s_.n_inner, f64s_.mixed,
-                                    f64s_.vars, f64s_.n_mixed, all_real_, diag_mode_, dcode_, dtab64_, x, y, s);
+        const FastVariant v = variant(16);
+        const bool st = v == FV_STAGED;
+        launch_fast<double, double>(*db_, st ? items_blk_ : items_, st ? n_items_blk_ : n_items_, iptr_, ient_, rbits_,
+                                    unif_, u_ar_, u_ai_, f64s_.outer, f64s_.n_outer, f64s_.outer_has_j, f64s_.inner,
+                                    f64s_.n_inner, f64s_.mixed, f64s_.vars, f64s_.n_mixed, all_real_, diag_mode_,
+                                    dcode_, dtab64_, x, y, s, v, st ? max_block_ * 16 : 0);
         return;
     }
     const DBuf& full = dfull64_;
@@ -903,11 +1317,26 @@ void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const 
         launch_spmv<uint32_t, double, double>(*db_, t64_, items_, n_items_, all_real_, diag_mode_, dcode_, dtab64_, full, x, y, s);
 }
 
+void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) const {
+    QKG_REQUIRE(fast(), "the device-resident Lanczos step needs the fast SpMV kernel");
+    const FastVariant v = variant(8);
+    const bool st = v == FV_STAGED;
+    launch_fast<float, float>(*db_, st ? items_blk_ : items_, st ? n_items_blk_ : n_items_, iptr_, ient_, rbits_, unif_,
+                              u_ar_, u_ai_, f32s_.outer, f32s_.n_outer, f32s_.outer_has_j, f32s_.inner, f32s_.n_inner,
+                              f32s_.mixed, f32s_.vars, f32s_.n_mixed, all_real_, diag_mode_, dcode_, dtab32_, nullptr,
+                              nullptr, s, v, st ? max_block_ * 8 : 0, &lz);
+}
+
+size_t Hamiltonian::lanczos_parts() const { return staged(8) ? n_items_blk_ : n_items_; }
+
 void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
     if (fast()) {
-        launch_fast<float, float>(*db_, items_, n_items_, iptr_, ient_, rbits_, unif_, u_ar_, u_ai_, f32s_.outer,
-                                  f32s_.n_outer, f32s_.outer_has_j, f32s_.inner, f32s_.n_inner, f32s_.mixed, f32s_.vars,
-                                  f32s_.n_mixed, all_real_, diag_mode_, dcode_, dtab32_, x, y, s);
+        const FastVariant v = variant(8);
+        const bool st = v == FV_STAGED;
+        launch_fast<float, float>(*db_, st ? items_blk_ : items_, st ? n_items_blk_ : n_items_, iptr_, ient_, rbits_,
+                                  unif_, u_ar_, u_ai_, f32s_.outer, f32s_.n_outer, f32s_.outer_has_j, f32s_.inner,
+                                  f32s_.n_inner, f32s_.mixed, f32s_.vars, f32s_.n_mixed, all_real_, diag_mode_, dcode_,
+                                  dtab32_, x, y, s, v, st ? max_block_ * 8 : 0);
         return;
     }
     if (wide_)

@@ -1,0 +1,412 @@
+// Device-resident mixed-precision Lanczos: one step = four kernels that read
+// the step index, the vector pointers and the recurrence scalars from device
+// memory, so the step is captured once as a CUDA graph and replayed.
+//
+// Stored vectors.  v_k = sig[k] * V_k with V_0 the normalised start vector and
+// V_{k+1} = w_k (the un-normalised residual of step k), sig[k+1] = 1 / beta_k.
+// The SpMV multiplies its output by sig[k], so y = H v_k and every stored
+// vector has norm beta_{k-1}: no growth, no separate normalisation pass.
+//   1. SpMV (fast kernel, Lanczos mode): V_{k+1} = sig_k H V_k, plus per-block
+//      partials of Re<V_k, V_{k+1}>  =>  alpha_k = sig_k * sum.
+//   2. lz_alpha: alpha_k; coefficients a = alpha_k sig_k, b = beta_{k-1} sig_{k-1}.
+//   3. lz_update: V_{k+1} -= a V_k + b V_{k-1}; compensated |V_{k+1}|^2 partials.
+//      (selective reorthogonalisation adds lz_proj, lz_proj_finish, lz_orth)
+//   4. lz_beta: beta_k, sig_{k+1}, k += 1.
+// alpha/beta are also written to mapped pinned host memory; the host reads
+// them a few steps behind the GPU (convergence test, selective
+// reorthogonalisation trigger) without stalling the stream.
+#include "solvers.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+namespace qkg {
+
+namespace {
+constexpr int kT = 256;
+constexpr int kUpdGrid = 152 * 8;
+constexpr int kTimedSteps = 8;  // steps launched one by one with an SpMV timer before the graph takes over
+constexpr int kInFlight = 6;    // steps the host lets the GPU run ahead of its checks
+
+struct LzState {
+    int k;
+    int pad;
+    double a, b;            // update coefficients of the current step
+    double pre, pim;        // projection on the Ritz vector (selective reorthogonalisation)
+};
+
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float t = hi + p;
+    const float z = t - hi;
+    lo += ((hi - (t - z)) + (p - z)) + e;
+    hi = t;
+}
+
+__device__ __forceinline__ double2 bsum2(double x, double y) {
+    __shared__ double2 sh[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, o);
+        y += __shfl_down_sync(0xffffffffu, y, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = make_double2(x, y);
+    __syncthreads();
+    double2 v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : make_double2(0.0, 0.0);
+    if (wid == 0)
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+        }
+    return v;
+}
+
+__global__ void lz_alpha_kernel(const double2* __restrict__ apart, int nparts, LzState* st, double* alpha,
+                                const double* beta, const double* sig, double* alpha_host) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += apart[i].x;
+    const double2 t = bsum2(s, 0.0);
+    if (threadIdx.x == 0) {
+        const int k = st->k;
+        const double a = sig[k] * t.x;
+        alpha[k] = a;
+        alpha_host[k] = a;
+        st->a = a * sig[k];
+        st->b = k > 0 ? beta[k - 1] * sig[k - 1] : 0.0;
+    }
+}
+
+__global__ void lz_update_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st, uint64_t n,
+                                 double2* __restrict__ bpart) {
+    const int k = st->k;
+    float2* __restrict__ w = static_cast<float2*>(vtab[k + 1]);
+    const float2* __restrict__ v = static_cast<const float2*>(vtab[k]);
+    const float2* __restrict__ vp = k > 0 ? static_cast<const float2*>(vtab[k - 1]) : nullptr;
+    const float a = (float)st->a, b = (float)st->b;
+    float hi = 0.f, lo = 0.f;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float2 x = w[i];
+        const float2 c = v[i];
+        x.x = fmaf(-a, c.x, x.x);
+        x.y = fmaf(-a, c.y, x.y);
+        if (vp) {
+            const float2 d = vp[i];
+            x.x = fmaf(-b, d.x, x.x);
+            x.y = fmaf(-b, d.y, x.y);
+        }
+        w[i] = x;
+        ff_acc(hi, lo, x.x, x.x);
+        ff_acc(hi, lo, x.y, x.y);
+    }
+    const double2 s = bsum2((double)hi + (double)lo, 0.0);
+    if (threadIdx.x == 0) bpart[blockIdx.x] = s;
+}
+
+// <psi, W> partials (complex) for selective reorthogonalisation.
+__global__ void lz_proj_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st,
+                               const float2* __restrict__ psi, uint64_t n, double2* __restrict__ ppart) {
+    const float2* __restrict__ w = static_cast<const float2*>(vtab[st->k + 1]);
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 a = psi[i], b = w[i];
+        ff_acc(rh, rl, a.x, b.x);
+        ff_acc(rh, rl, a.y, b.y);
+        ff_acc(ih, il, a.x, b.y);
+        ff_acc(ih, il, -a.y, b.x);
+    }
+    const double2 s = bsum2((double)rh + (double)rl, (double)ih + (double)il);
+    if (threadIdx.x == 0) ppart[blockIdx.x] = s;
+}
+__global__ void lz_proj_finish_kernel(const double2* __restrict__ ppart, int nparts, LzState* st) {
+    double r = 0.0, i = 0.0;
+    for (int j = threadIdx.x; j < nparts; j += blockDim.x) {
+        r += ppart[j].x;
+        i += ppart[j].y;
+    }
+    const double2 t = bsum2(r, i);
+    if (threadIdx.x == 0) {
+        st->pre = t.x;
+        st->pim = t.y;
+    }
+}
+// W -= c psi with c = <psi, W>; |W|^2 partials.
+__global__ void lz_orth_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st,
+                               const float2* __restrict__ psi, uint64_t n, double2* __restrict__ bpart) {
+    float2* __restrict__ w = static_cast<float2*>(vtab[st->k + 1]);
+    const float cr = (float)st->pre, ci = (float)st->pim;
+    float hi = 0.f, lo = 0.f;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 p = psi[i];
+        float2 x = w[i];
+        x.x -= cr * p.x - ci * p.y;
+        x.y -= cr * p.y + ci * p.x;
+        w[i] = x;
+        ff_acc(hi, lo, x.x, x.x);
+        ff_acc(hi, lo, x.y, x.y);
+    }
+    const double2 s = bsum2((double)hi + (double)lo, 0.0);
+    if (threadIdx.x == 0) bpart[blockIdx.x] = s;
+}
+
+__global__ void lz_beta_kernel(const double2* __restrict__ bpart, int nparts, LzState* st, double* beta, double* sig,
+                               double* beta_host) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += bpart[i].x;
+    const double2 t = bsum2(s, 0.0);
+    if (threadIdx.x == 0) {
+        const int k = st->k;
+        const double b = sqrt(t.x);
+        beta[k] = b;
+        beta_host[k] = b;
+        sig[k + 1] = b > 0.0 ? 1.0 / b : 0.0;
+        st->k = k + 1;
+    }
+}
+
+using clk = std::chrono::steady_clock;
+inline double secs(clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+struct Mapped {
+    double* h = nullptr;
+    double* d = nullptr;
+    explicit Mapped(size_t n) {
+        QKG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&h), n * sizeof(double), cudaHostAllocMapped));
+        QKG_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&d), h, 0));
+        std::fill(h, h + n, 0.0);
+    }
+    ~Mapped() { if (h) cudaFreeHost(h); }
+};
+}  // namespace
+
+bool lanczos_device_supported(const Hamiltonian& H) { return H.fast(); }
+
+LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
+    LanczosOut out;
+    const uint64_t n = H.dim();
+    if (n == 0) return out;
+    cudaStream_t st = H.stream();
+    const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
+    if (nmax <= 0) return out;
+    // all nmax + 1 Krylov vectors (FP32) up front: the graph addresses them through vtab
+    size_t fr = 0, tot = 0;
+    QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+    const size_t need = (size_t)(nmax + 1) * n * sizeof(float2);
+    if (need + (512ull << 20) > fr)
+        throw Error(CUDA_ERR, "out of device memory for " + std::to_string(nmax + 1) + " Krylov vectors");
+    std::vector<DBuf> V;
+    V.reserve(nmax + 1);
+    std::vector<void*> vptr;
+    for (int i = 0; i <= nmax; ++i) {
+        V.emplace_back(n * sizeof(float2));
+        vptr.push_back(V.back().p);
+    }
+    DBuf vtab((nmax + 1) * sizeof(void*));
+    QKG_CUDA(cudaMemcpy(vtab.p, vptr.data(), vptr.size() * sizeof(void*), cudaMemcpyHostToDevice));
+    DBuf state(sizeof(LzState)), alpha((nmax + 2) * 8), beta((nmax + 2) * 8), sig((nmax + 2) * 8);
+    DBuf apart(std::max<size_t>(1, H.lanczos_parts()) * sizeof(double2)), bpart(kUpdGrid * sizeof(double2)),
+        ppart(kUpdGrid * sizeof(double2));
+    Mapped ah(nmax + 2), bh(nmax + 2);
+    Workspace ws(std::max<size_t>(1 << 16, (size_t)1216 * (size_t)(nmax + 2)));
+    DBuf tmp;
+
+    float2* v0 = static_cast<float2*>(vptr[0]);
+    if (o.device_start) {
+        philox_normal_f32(o.seed, 0, v0, n, st);
+    } else {
+        std::vector<cd> h(n);
+        if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
+        else ref_uniform_complex(1234, n, h.data(), o.f32_stream);
+        DBuf d64(n * sizeof(double2)), t64(n * sizeof(double2));
+        QKG_CUDA(cudaMemcpyAsync(t64.p, h.data(), n * sizeof(double2), cudaMemcpyHostToDevice, st));
+        H.to_internal_f64(t64.as<double2>(), d64.as<double2>(), st);
+        f64_to_f32(d64.as<double2>(), v0, n, st);
+        QKG_CUDA(cudaStreamSynchronize(st));
+    }
+    const double nr0 = std::sqrt(nrm2sq_f32(v0, n, ws, st));
+    if (nr0 != 0.0) scal_f32(1.0 / nr0, v0, n, st);
+    {
+        LzState s0{};
+        const double one = 1.0;
+        QKG_CUDA(cudaMemcpyAsync(state.p, &s0, sizeof(s0), cudaMemcpyHostToDevice, st));
+        QKG_CUDA(cudaMemcpyAsync(sig.p, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+        QKG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    LanczosHooks hooks;
+    hooks.vtab = static_cast<const void* const*>(vtab.p);
+    hooks.kstep = &state.as<LzState>()->k;
+    hooks.sig = sig.as<double>();
+    hooks.apart = apart.as<double2>();
+    const int nparts = (int)H.lanczos_parts();
+    DBuf psi;  // selective reorthogonalisation vector (once active)
+    auto enqueue_step = [&](bool so, LaunchTimer* timer) {
+        if (timer) timer->start();
+        H.apply_lanczos_f32(hooks, st);
+        if (timer) timer->stop();
+        lz_alpha_kernel<<<1, kT, 0, st>>>(apart.as<double2>(), nparts, state.as<LzState>(), alpha.as<double>(),
+                                          beta.as<double>(), sig.as<double>(), ah.d);
+        QKG_LAUNCHED();
+        lz_update_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
+                                                  bpart.as<double2>());
+        QKG_LAUNCHED();
+        if (so) {
+            lz_proj_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(),
+                                                    psi.as<float2>(), n, ppart.as<double2>());
+            QKG_LAUNCHED();
+            lz_proj_finish_kernel<<<1, kT, 0, st>>>(ppart.as<double2>(), kUpdGrid, state.as<LzState>());
+            QKG_LAUNCHED();
+            lz_orth_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(),
+                                                    psi.as<float2>(), n, bpart.as<double2>());
+            QKG_LAUNCHED();
+        }
+        lz_beta_kernel<<<1, kT, 0, st>>>(bpart.as<double2>(), kUpdGrid, state.as<LzState>(), beta.as<double>(),
+                                         sig.as<double>(), bh.d);
+        QKG_LAUNCHED();
+    };
+    auto capture = [&](bool so) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        QKG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(so, nullptr);
+        QKG_CUDA(cudaStreamEndCapture(st, &g));
+        QKG_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        QKG_CUDA(cudaGraphDestroy(g));
+        return ge;
+    };
+    const int kernels_plain = 4, kernels_so = 7;
+    cudaGraphExec_t g_plain = nullptr, g_so = nullptr;
+    std::vector<cudaEvent_t> ev(kInFlight + 2);
+    for (auto& e : ev) QKG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+
+    bool so_active = false;
+    int stop_at = -1;       // last accepted step (inclusive)
+    bool converged = false;
+    double e_old = 1e100;
+    const double so_tol = 3.5e-4;
+    LaunchTimer timer(st);
+    int launched = 0, checked = 0;
+    const auto t0 = clk::now();
+    try {
+        auto check_step = [&](int j) {  // step j has completed
+            const double b = bh.h[j];
+            if (b < 1e-15) { converged = true; stop_at = j; return; }
+            if (j + 1 == nmax) { stop_at = j; return; }
+            if (j > 0) {
+                std::vector<double> a(ah.h, ah.h + j + 1), bb(bh.h, bh.h + j);
+                const double e = tridiag_lowest(a.data(), bb.data(), j + 1);
+                if (!o.fixed_steps && std::abs(e - e_old) < o.tol) { converged = true; stop_at = j; return; }
+                e_old = e;
+                if (!so_active && j + 1 >= 4) {
+                    std::vector<double> d, z;
+                    tridiag_eig(a.data(), bb.data(), j + 1, d, {j}, z);
+                    int mi = 0;
+                    for (int q = 1; q <= j; ++q) if (d[q] < d[mi]) mi = q;
+                    double tn = 0.0;
+                    for (double x : d) tn = std::max(tn, std::abs(x));
+                    if (b * std::abs(z[mi]) <= so_tol * tn) {
+                        // Ritz vector of T_j from v_0..v_j = sig_i V_i (sig_0 = 1, sig_{i+1} = 1/beta_i)
+                        std::vector<double> s;
+                        tridiag_ground(a.data(), bb.data(), j + 1, s);
+                        std::vector<cd> c(j + 1);
+                        double sg = 1.0;
+                        for (int i = 0; i <= j; ++i) {
+                            c[i] = s[i] * sg;
+                            sg = 1.0 / bh.h[i];
+                        }
+                        psi.alloc(n * sizeof(float2));
+                        QKG_CUDA(cudaMemsetAsync(psi.p, 0, n * sizeof(float2), st));
+                        mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), j + 1, c.data(), psi.as<float2>(),
+                                     n, ws, st);
+                        const double pn = std::sqrt(nrm2sq_f32(psi.as<float2>(), n, ws, st));
+                        scal_f32(1.0 / pn, psi.as<float2>(), n, st);
+                        so_active = true;
+                    }
+                }
+            }
+        };
+        while (launched < nmax && stop_at < 0) {
+            if (launched < kTimedSteps) {
+                enqueue_step(so_active, &timer);
+                out.t_spmv += timer.collect();  // waits for this SpMV only
+                ++out.n_spmv;
+            } else {
+                cudaGraphExec_t& g = so_active ? g_so : g_plain;
+                if (!g) g = capture(so_active);
+                QKG_CUDA(cudaGraphLaunch(g, st));
+                for (int q = 0; q < (so_active ? kernels_so : kernels_plain); ++q) count_launch();
+            }
+            if (so_active) ++out.n_selective;
+            QKG_CUDA(cudaEventRecord(ev[launched % ev.size()], st));
+            ++launched;
+            while (checked < launched && stop_at < 0) {
+                cudaEvent_t e = ev[checked % ev.size()];
+                if (launched - checked < kInFlight) {
+                    const cudaError_t q = cudaEventQuery(e);
+                    if (q == cudaErrorNotReady) break;
+                    QKG_CUDA(q);
+                } else {
+                    QKG_CUDA(cudaEventSynchronize(e));
+                }
+                check_step(checked);
+                ++checked;
+            }
+        }
+        QKG_CUDA(cudaStreamSynchronize(st));
+        while (stop_at < 0 && checked < launched) check_step(checked++);
+    } catch (...) {
+        cudaStreamSynchronize(st);
+        for (auto& e : ev) cudaEventDestroy(e);
+        if (g_plain) cudaGraphExecDestroy(g_plain);
+        if (g_so) cudaGraphExecDestroy(g_so);
+        throw;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (g_plain) cudaGraphExecDestroy(g_plain);
+    if (g_so) cudaGraphExecDestroy(g_so);
+    out.t_loop = secs(t0, clk::now());
+    if (stop_at < 0) stop_at = launched - 1;
+    out.iters = stop_at + 1;
+    out.converged = converged;
+    out.alphas.assign(ah.h, ah.h + stop_at + 1);
+    out.betas.assign(bh.h, bh.h + stop_at);  // the last step's beta is not part of T
+
+    // Ritz vector from the FP32 basis, then FP64 Rayleigh quotient and residual.
+    const auto t1 = clk::now();
+    std::vector<double> s;
+    out.energy_tridiag = tridiag_ground(out.alphas.data(), out.betas.data(), (int)out.alphas.size(), s);
+    std::vector<cd> c(s.size());
+    double sg = 1.0;
+    for (size_t i = 0; i < s.size(); ++i) {
+        c[i] = s[i] * sg;
+        sg = 1.0 / bh.h[i];
+    }
+    DBuf r32(n * sizeof(float2)), r64(n * sizeof(double2)), h64(n * sizeof(double2));
+    QKG_CUDA(cudaMemsetAsync(r32.p, 0, n * sizeof(float2), st));
+    mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), (int)c.size(), c.data(), r32.as<float2>(), n, ws, st);
+    f32_to_f64(r32.as<float2>(), r64.as<double2>(), n, st);
+    const double nr = std::sqrt(nrm2sq_f64(r64.as<double2>(), n, ws, st));
+    scal_f64(1.0 / nr, r64.as<double2>(), n, st);
+    H.apply_f64(r64.as<double2>(), h64.as<double2>(), st);
+    const double E = dot_f64(r64.as<double2>(), h64.as<double2>(), n, ws, st).real();
+    axpy_f64(-E, r64.as<double2>(), h64.as<double2>(), n, st);
+    out.residual = std::sqrt(nrm2sq_f64(h64.as<double2>(), n, ws, st));
+    out.energy = E;
+    out.t_refine = secs(t1, clk::now());
+    if (o.want_vec) {
+        out.evec.resize(n);
+        DBuf t2(n * sizeof(double2));
+        const double2* src = r64.as<double2>();
+        if (H.permuted()) {
+            H.to_reference_f64(r64.as<double2>(), t2.as<double2>(), st);
+            src = t2.as<double2>();
+        }
+        QKG_CUDA(cudaMemcpyAsync(out.evec.data(), src, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        QKG_CUDA(cudaStreamSynchronize(st));
+    }
+    return out;
+}
+
+}  // namespace qkg

@@ -374,6 +374,12 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
     LanczosOut out;
     const uint64_t n = H.dim();
     if (n == 0) return out;
+    if (lanczos_device_supported(H)) {
+        size_t fr = 0, tot = 0;
+        QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+        const uint64_t k = std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n) + 1;
+        if (k * n * sizeof(float2) + (1ull << 30) < fr) return lanczos_mixed_device(H, o);
+    }
     cudaStream_t st = H.stream();
     const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
     Workspace ws(ws_cap(nmax + 2));

@@ -82,6 +82,10 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o);
 // selective reorthogonalisation against the converged Ritz vector, FP64
 // Rayleigh-quotient + residual refinement at the end.
 LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o);
+// The same mixed form with a device-resident recurrence (one CUDA graph per
+// step); needs the fast SpMV kernel and room for maxiter + 1 FP32 vectors.
+bool lanczos_device_supported(const Hamiltonian& H);
+LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o);
 
 // ---- continued fraction (src/solvers/dynamics.cpp:13-89) --------------------------
 struct CFOut { std::vector<double> alphas, betas; double norm = 0.0; };

@@ -133,6 +133,28 @@ def test_mixed_form_matches_fp64(qk, L):
     assert ov > 1 - 1e-8
 
 
+@pytest.mark.parametrize("m", [M.heisenberg(18, True, 0), M.hubbard(8, True, 4, 4),
+                               (M.FERMION, 16, M.sector(n=6), M.fermion_chain_terms(16, True))])
+def test_mixed_device_engine_matches_host_driven(qk, m):
+    """The device-resident mixed Lanczos (graph-replayed steps, fast kernel)
+    and the host-driven mixed Lanczos (generic kernel) reach the same E0, and
+    both match FP64 to 1e-10 relative; fixed-step runs report every step."""
+    b, s, o = make_model(qk, *m)
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    assert H.select_kernel(False)
+    r_dev = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12, mixed=True)
+    r64 = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12)
+    H.select_kernel(True)
+    r_host = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12, mixed=True)
+    for r in (r_dev, r_host):
+        assert abs(r.energy - r64.energy) <= 1e-10 * abs(r64.energy)
+        assert r.residual < 1e-4
+    H.select_kernel(False)
+    f = qk.lanczos_fixed_steps(H, 60, seed=3, mixed=True)
+    assert f.iterations == 60 and f.spmv_calls >= 1
+    assert abs(f.energy - r64.energy) <= 1e-10 * abs(r64.energy)
+
+
 def test_lanczos_from_given_start_matches_oracle(qk, oracle):
     """Same start vector on both sides: E0 and iteration count of the
     reference algorithm (oracle restatement) are reproduced."""

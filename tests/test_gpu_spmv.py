@@ -83,12 +83,12 @@ def test_entries_bit_exact(qk, name):
     np.testing.assert_allclose(vals, g["csr_vals"], rtol=0, atol=1e-15)
 
 
-@pytest.mark.parametrize("generic", [False, True], ids=["fast", "generic"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4], ids=["auto", "generic", "fast", "fast-staged", "fast-rows4"])
 @pytest.mark.parametrize("name", golden_names())
-def test_apply_and_diagonal(qk, name, generic):
+def test_apply_and_diagonal(qk, name, mode):
     g = load_golden(name)
     H = gpu_ham(qk, g)
-    H.select_kernel(generic)
+    H.select_kernel(mode=mode)
     assert H.dimension == int(g["dim"])
     np.testing.assert_array_equal(H.diagonal(), g["diag"].real)  # summed in term order: bit-exact
     if "x" in g:
@@ -125,8 +125,8 @@ def test_apply_against_oracle(qk, oracle, model, N, sector, terms):
     rng = np.random.default_rng(7)
     x = rng.normal(size=o.dim) + 1j * rng.normal(size=o.dim)
     yo = o.apply(x)
-    for generic in (False, True):
-        H.select_kernel(generic)
+    for mode in (0, 1, 2, 3, 4):
+        H.select_kernel(mode=mode)
         y = H.apply(x)
         assert np.abs(y - yo).max() <= RTOL64 * np.abs(yo).max()
         y32 = apply32(qk, H, x)
