@@ -288,6 +288,58 @@ int qkrylov_hamiltonian_benchmark_apply(qkrylov_hamiltonian_h h, int fp32, int r
 int qkrylov_hamiltonian_entries(qkrylov_hamiltonian_h h, uint64_t* nnz_out, uint64_t* row_offsets, uint64_t* cols,
                                 double* vals);
 
+/* ---- batched Lanczos over block vectors (GB300 additions) -------------------
+ * Several Hamiltonians (e.g. every Sz sector of one chain) with n_vec vectors
+ * each are advanced together: every Lanczos step is one block-SpMV launch for
+ * all of them (vectors interleaved by row), with all scalars on the device and
+ * the steps replayed as a CUDA graph.  The recurrence per vector is the
+ * reference's compute_tridiag / continued_fraction_coeffs loop
+ * (src/solvers/ftlm.cpp:24-53, src/solvers/dynamics.cpp:13-59), including its
+ * stop at beta < 1e-15.  mixed != 0: FP32 vectors and SpMV, compensated
+ * reductions combined in FP64; mixed == 0: FP64 throughout.  Needs every
+ * Hamiltonian on the fast SpMV kernel (32-bit states) and on one device. */
+#define QKRYLOV_START_FTLM_STREAM 0     /* mt19937(42) complex normal per Hamiltonian (ftlm.cpp:133-143) */
+#define QKRYLOV_START_PHILOX 1          /* seeded Philox Gaussian vectors generated on the device */
+#define QKRYLOV_START_GIVEN 2           /* caller's vectors, reference order */
+#define QKRYLOV_START_FTLM_STREAM_F32 3 /* the FTLM stream through normal_distribution<float> */
+
+typedef struct {
+    double seconds;         /* device time of the Lanczos loop (CUDA events; start vectors excluded) */
+    double spmv_ms;         /* mean CUDA-event time of one block SpMV launch (first steps) */
+    int vectors_per_lane;   /* block-SpMV tile shape picked by the autotuner (1, 2 or 4) */
+    int padded_vectors;     /* vectors per row in the block (n_vec rounded up to a power of two) */
+    uint64_t rows;          /* sum of the Hamiltonians' dimensions */
+    double tune_ms[3];      /* autotuner timings for 1, 2, 4 vectors per lane (0: not measured) */
+} qkrylov_block_stats_t;
+
+/* Tridiagonals of n_ham * n_vec vectors (vector i = h * n_vec + v), n_steps
+ * steps each.  start_vectors (QKRYLOV_START_GIVEN): for each Hamiltonian in
+ * order, n_vec vectors of its dimension, complex interleaved [re, im].
+ * alphas/betas: [i * n_steps + k]; n_alpha/n_beta: counts recorded per vector;
+ * norm2: squared norm of each start vector.  stats is optional. */
+int qkrylov_block_lanczos_tridiag(const qkrylov_hamiltonian_h* hams, int n_ham, int n_vec, int n_steps, int mixed,
+                                  int start_kind, uint64_t seed, const double* start_vectors, double* alphas,
+                                  double* betas, int* n_alpha, int* n_beta, double* norm2,
+                                  qkrylov_block_stats_t* stats);
+
+/* FTLM (ftlm.cpp:123-170) summed over Hamiltonians: Z = sum_h Z_h,
+ * E = sum_h Z_h E_h / Z, Cv = beta^2 (<E^2> - <E>^2), n_random vectors per
+ * Hamiltonian (<= 32) in one batched run, evaluated at n_beta inverse
+ * temperatures.  log_shift (optional, n_beta): shifted evaluation, the true
+ * partition function is Z * exp(log_shift). */
+int qkrylov_ftlm_sectors_f64(const qkrylov_hamiltonian_h* hams, int n_ham, const double* betas, int n_beta,
+                             int n_random, int n_steps, int mixed, int start_kind, uint64_t seed, double* Z, double* E,
+                             double* Cv, double* log_shift, qkrylov_block_stats_t* stats);
+
+/* Continued-fraction coefficients (dynamics.cpp:13-59) of n_rhs right-hand
+ * sides (<= 32; phi0: n_rhs vectors of the Hamiltonian's dimension, reference
+ * order, complex interleaved) in one batched run.  alphas/betas
+ * [r * n_iter + k], n_alpha/n_beta counts, norms: ||phi0_r|| (0 for a zero
+ * vector, which gets no coefficients). */
+int qkrylov_cf_block_f64(qkrylov_hamiltonian_h h, const double* phi0, int n_rhs, int n_iter, int mixed,
+                         double* alphas, double* betas, int* n_alpha, int* n_beta, double* norms,
+                         qkrylov_block_stats_t* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,9 +46,19 @@ class FTLMResultF64(_c.Structure):
     _fields_ = [("beta", _d), ("partition_function", _d), ("internal_energy", _d), ("specific_heat", _d)]
 
 
+class BlockStatsC(_c.Structure):
+    _fields_ = [("seconds", _d), ("spmv_ms", _d), ("vectors_per_lane", _i), ("padded_vectors", _i), ("rows", _u64),
+                ("tune_ms", _d * 3)]
+
+
+START_FTLM_STREAM, START_PHILOX, START_GIVEN, START_FTLM_STREAM_F32 = 0, 1, 2, 3
+
 # name: (restype, argtypes)
 _SIGS = {
     "qkrylov_last_error": (_c.c_char_p, []),
+    "qkrylov_block_lanczos_tridiag": (_i, [_vp, _i, _i, _i, _i, _i, _u64, _dp, _dp, _dp, _ip, _ip, _dp, _vp]),
+    "qkrylov_ftlm_sectors_f64": (_i, [_vp, _i, _dp, _i, _i, _i, _i, _i, _u64, _dp, _dp, _dp, _dp, _vp]),
+    "qkrylov_cf_block_f64": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, _ip, _ip, _dp, _vp]),
     "qkrylov_sector_create": (_vp, []),
     "qkrylov_sector_destroy": (None, [_vp]),
     "qkrylov_sector_set_sz": (_i, [_vp, _i]),
@@ -511,6 +521,104 @@ def ftlm(H, beta, n_random=50, n_steps=100, shifted=False):
     if _np.ndim(beta) == 0:
         return FTLMResult(float(b[0]), float(Z[0]), float(E[0]), float(C[0]), float(ls[0]) if shifted else None)
     return FTLMResult(b, Z, E, C, ls)
+
+
+# ------------------------------------------------------------------ batched Lanczos
+_STARTS = {"ftlm": START_FTLM_STREAM, "philox": START_PHILOX, "given": START_GIVEN, "ftlm32": START_FTLM_STREAM_F32}
+
+
+def _stats(st):
+    return {"seconds": st.seconds, "spmv_ms": st.spmv_ms, "vectors_per_lane": st.vectors_per_lane,
+            "padded_vectors": st.padded_vectors, "rows": int(st.rows), "tune_ms": list(st.tune_ms)}
+
+
+def _ham_array(hams):
+    hams = list(hams)
+    arr = (_c.c_void_p * len(hams))(*[h._h for h in hams])
+    return hams, arr
+
+
+class BlockTridiagResult:
+    """Per vector i = h * n_vec + v: alphas[i], betas[i] (the recorded
+    coefficients), norm2[i] (squared norm of its start vector); stats of the
+    batched run (device seconds, block-SpMV time, tile shape)."""
+
+    def __init__(self, alphas, betas, norm2, stats):
+        self.alphas, self.betas, self.norm2, self.stats = alphas, betas, norm2, stats
+
+
+def block_lanczos_tridiag(hams, n_vec, n_steps, mixed=True, start="ftlm", seed=0, start_vectors=None):
+    """Three-term Lanczos (no reorthogonalisation, stop at beta < 1e-15) of
+    n_vec vectors for each Hamiltonian in ``hams``, all advanced together by
+    one block-SpMV launch per step.  ``start``: "ftlm" (the reference FTLM
+    stream, mt19937(42) per Hamiltonian), "ftlm32" (its float variant),
+    "philox" (device Gaussian vectors from ``seed``) or "given"
+    (``start_vectors``: per Hamiltonian an (n_vec, dim) complex array)."""
+    hams, arr = _ham_array(hams)
+    kind = _STARTS[start]
+    buf = None
+    if kind == START_GIVEN:
+        parts = []
+        for h, sv in zip(hams, start_vectors):
+            a = _np.ascontiguousarray(sv, dtype=_np.complex128).reshape(n_vec, h.dimension)
+            parts.append(a.ravel())
+        buf = _np.ascontiguousarray(_np.concatenate(parts))
+    nv = len(hams) * n_vec
+    a = _np.zeros(nv * max(1, n_steps))
+    b = _np.zeros(nv * max(1, n_steps))
+    na = _np.zeros(nv, dtype=_np.int32)
+    nb = _np.zeros(nv, dtype=_np.int32)
+    n2 = _np.zeros(nv)
+    st = BlockStatsC()
+    _check(lib().qkrylov_block_lanczos_tridiag(arr, len(hams), int(n_vec), int(n_steps), int(bool(mixed)), kind,
+                                               int(seed), _dptr(buf.view(_np.float64)) if buf is not None else None,
+                                               _dptr(a), _dptr(b), na.ctypes.data_as(_ip), nb.ctypes.data_as(_ip),
+                                               _dptr(n2), _c.byref(st)))
+    a = a.reshape(nv, -1)
+    b = b.reshape(nv, -1)
+    return BlockTridiagResult([a[i, : na[i]].copy() for i in range(nv)], [b[i, : nb[i]].copy() for i in range(nv)],
+                              n2, _stats(st))
+
+
+class FTLMSectorsResult:
+    def __init__(self, beta, Z, E, Cv, log_shift, stats):
+        self.beta, self.partition_function, self.internal_energy = beta, Z, E
+        self.specific_heat, self.log_shift, self.stats = Cv, log_shift, stats
+
+
+def ftlm_sectors(hams, beta, n_random=32, n_steps=100, mixed=True, start="ftlm", seed=0, shifted=False):
+    """FTLM summed over several Hamiltonians (e.g. all Sz sectors), every
+    sector's n_random vectors in one batched run: Z = sum of the per-sector
+    reference estimates (ftlm.cpp:123-170), E and Cv of the combined ensemble."""
+    hams, arr = _ham_array(hams)
+    b = _np.atleast_1d(_np.asarray(beta, dtype=_np.float64))
+    Z, E, C = _np.zeros_like(b), _np.zeros_like(b), _np.zeros_like(b)
+    ls = _np.zeros_like(b) if shifted else None
+    st = BlockStatsC()
+    _check(lib().qkrylov_ftlm_sectors_f64(arr, len(hams), _dptr(b), b.size, int(n_random), int(n_steps),
+                                          int(bool(mixed)), _STARTS[start], int(seed), _dptr(Z), _dptr(E), _dptr(C),
+                                          _dptr(ls) if shifted else None, _c.byref(st)))
+    return FTLMSectorsResult(b, Z, E, C, ls, _stats(st))
+
+
+def continued_fraction_block(H, phi0s, n_iter=100, mixed=True):
+    """continued_fraction_coeffs for several right-hand sides (<= 32) in one
+    batched run; returns ([DynamicsResult per right-hand side], stats)."""
+    n = H.dimension
+    P = _np.ascontiguousarray(_np.asarray(phi0s, dtype=_np.complex128).reshape(-1, n))
+    r = P.shape[0]
+    a = _np.zeros(r * max(1, n_iter))
+    b = _np.zeros(r * max(1, n_iter))
+    na = _np.zeros(r, dtype=_np.int32)
+    nb = _np.zeros(r, dtype=_np.int32)
+    nr = _np.zeros(r)
+    st = BlockStatsC()
+    _check(lib().qkrylov_cf_block_f64(H._h, _dptr(P.view(_np.float64)), r, int(n_iter), int(bool(mixed)), _dptr(a),
+                                      _dptr(b), na.ctypes.data_as(_ip), nb.ctypes.data_as(_ip), _dptr(nr),
+                                      _c.byref(st)))
+    a = a.reshape(r, -1)
+    b = b.reshape(r, -1)
+    return [DynamicsResult(a[i, : na[i]].copy(), b[i, : nb[i]].copy(), float(nr[i])) for i in range(r)], _stats(st)
 
 
 # ------------------------------------------------------------------ expression sugar

@@ -70,6 +70,7 @@ constexpr int kMaxTableBits = 22;
 std::atomic<uint64_t> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void add_launches(int64_t d) { g_launches.fetch_add((uint64_t)d, std::memory_order_relaxed); }
 
 void set_last_error(const std::string& msg) { t_last_error = msg; }
 const char* last_error() { return t_last_error.c_str(); }

@@ -5,10 +5,12 @@
 #include "../../include/qkrylov_c_api.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <mutex>
 
+#include "block.hpp"
 #include "solvers.hpp"
 
 using qkg::cd;
@@ -645,6 +647,112 @@ int qkrylov_ftlm_multi_beta_f64(qkrylov_hamiltonian_h h, const double* betas, in
         const auto tri = qkg::ftlm_tridiags_f64(*h->ptr, n_random, n_steps);
         qkg::ftlm_observables(tri, betas, n_beta, Z, E, Cv, log_shift != nullptr, log_shift);
     });
+}
+
+}  // extern "C"
+
+// ---- batched Lanczos over block vectors ------------------------------------------
+namespace {
+bool collect_hams(const qkrylov_hamiltonian_h* hams, int n, std::vector<qkg::Hamiltonian*>& hs) {
+    if (!hams || n <= 0) return false;
+    for (int i = 0; i < n; ++i) {
+        if (!hams[i] || !hams[i]->ptr) return false;
+        hs.push_back(hams[i]->ptr.get());
+    }
+    return true;
+}
+void fill_stats(const qkg::BlockTridiag& t, qkrylov_block_stats_t* st) {
+    if (!st) return;
+    st->seconds = t.seconds;
+    st->spmv_ms = t.spmv_ms;
+    st->vectors_per_lane = t.vpl;
+    st->padded_vectors = t.rp;
+    st->rows = t.rows;
+    for (int i = 0; i < 3; ++i) st->tune_ms[i] = i < (int)t.tune_ms.size() ? t.tune_ms[i] : 0.0;
+}
+qkg::BlockOpts block_opts(int n_vec, int n_steps, int mixed, int start_kind, uint64_t seed) {
+    qkg::BlockOpts o;
+    o.R = n_vec;
+    o.steps = n_steps;
+    o.mixed = mixed != 0;
+    o.seed = seed;
+    switch (start_kind) {
+        case QKRYLOV_START_FTLM_STREAM: o.start = qkg::BlockStart::FtlmStream; break;
+        case QKRYLOV_START_FTLM_STREAM_F32: o.start = qkg::BlockStart::FtlmStream; o.f32_stream = true; break;
+        case QKRYLOV_START_PHILOX: o.start = qkg::BlockStart::Philox; break;
+        case QKRYLOV_START_GIVEN: o.start = qkg::BlockStart::Given; break;
+        default: throw qkg::Error(QKRYLOV_ERROR_INVALID_ARG, "unknown start kind");
+    }
+    return o;
+}
+}  // namespace
+
+extern "C" {
+
+int qkrylov_block_lanczos_tridiag(const qkrylov_hamiltonian_h* hams, int n_ham, int n_vec, int n_steps, int mixed,
+                                  int start_kind, uint64_t seed, const double* start_vectors, double* alphas,
+                                  double* betas, int* n_alpha, int* n_beta, double* norm2,
+                                  qkrylov_block_stats_t* stats) {
+    std::vector<qkg::Hamiltonian*> hs;
+    if (!collect_hams(hams, n_ham, hs) || n_vec < 1 || n_vec > 32 || n_steps < 0 || !alphas || !betas || !n_alpha ||
+        !n_beta || !norm2 || (start_kind == QKRYLOV_START_GIVEN && !start_vectors))
+        return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        set_device(hams[0]);
+        qkg::BlockOpts o = block_opts(n_vec, n_steps, mixed, start_kind, seed);
+        if (o.start == qkg::BlockStart::Given) {
+            const cd* p = reinterpret_cast<const cd*>(start_vectors);
+            for (auto* H : hs)
+                for (int v = 0; v < n_vec; ++v) {
+                    o.given.push_back(p);
+                    p += H->dim();
+                }
+        }
+        const qkg::BlockTridiag t = qkg::block_lanczos(hs, o);
+        const size_t nv = (size_t)n_ham * n_vec;
+        for (size_t i = 0; i < nv; ++i) {
+            n_alpha[i] = (int)t.alpha[i].size();
+            n_beta[i] = (int)t.beta[i].size();
+            norm2[i] = t.norm2[i];
+            for (int k = 0; k < n_steps; ++k) {
+                alphas[i * n_steps + k] = k < n_alpha[i] ? t.alpha[i][k] : 0.0;
+                betas[i * n_steps + k] = k < n_beta[i] ? t.beta[i][k] : 0.0;
+            }
+        }
+        fill_stats(t, stats);
+    });
+}
+
+int qkrylov_ftlm_sectors_f64(const qkrylov_hamiltonian_h* hams, int n_ham, const double* betas, int n_beta,
+                             int n_random, int n_steps, int mixed, int start_kind, uint64_t seed, double* Z, double* E,
+                             double* Cv, double* log_shift, qkrylov_block_stats_t* stats) {
+    std::vector<qkg::Hamiltonian*> hs;
+    if (!collect_hams(hams, n_ham, hs) || !betas || n_beta < 0 || n_random < 1 || n_random > 32 || n_steps < 0 ||
+        !Z || !E || !Cv || start_kind == QKRYLOV_START_GIVEN)
+        return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        set_device(hams[0]);
+        const qkg::BlockTridiag t = qkg::block_lanczos(hs, block_opts(n_random, n_steps, mixed, start_kind, seed));
+        qkg::ftlm_observables_block(t, betas, n_beta, Z, E, Cv, log_shift != nullptr, log_shift);
+        fill_stats(t, stats);
+    });
+}
+
+int qkrylov_cf_block_f64(qkrylov_hamiltonian_h h, const double* phi0, int n_rhs, int n_iter, int mixed,
+                         double* alphas, double* betas, int* n_alpha, int* n_beta, double* norms,
+                         qkrylov_block_stats_t* stats) {
+    if (!h || !h->ptr || !phi0 || n_rhs < 1 || n_rhs > 32 || n_iter < 0 || !alphas || !betas || !n_alpha || !n_beta ||
+        !norms)
+        return QKRYLOV_ERROR_INVALID_ARG;
+    std::vector<double> n2((size_t)n_rhs);
+    const int rc = qkrylov_block_lanczos_tridiag(&h, 1, n_rhs, n_iter, mixed, QKRYLOV_START_GIVEN, 0, phi0, alphas,
+                                                 betas, n_alpha, n_beta, n2.data(), stats);
+    if (rc == QKRYLOV_SUCCESS)
+        for (int i = 0; i < n_rhs; ++i) {
+            const double nr = std::sqrt(n2[i]);
+            norms[i] = nr < 1e-15 ? 0.0 : nr;  // dynamics.cpp:27: a zero right-hand side has no coefficients
+        }
+    return rc;
 }
 
 }  // extern "C"

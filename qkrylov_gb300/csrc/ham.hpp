@@ -43,6 +43,10 @@ struct LanczosHooks {
     double2* apart = nullptr;
 };
 
+namespace fastk {
+template <class A> struct FastParams;
+}
+
 // Per-precision copy of the compiled term lists.
 struct TermSet {
     DBuf outer, inner, mixed, diag, all, vars;
@@ -112,6 +116,13 @@ public:
     // autotuner record: mean ms of [precision][variant] (0 when not measured)
     double tuned_ms(int prec, int v) const { return tune_ms_[prec][v]; }
     size_t inner_table_entries() const { return n_ient_; }
+    // Fast-kernel parameters (one work item per <= 1024 rows of an outer
+    // block) for arithmetic type A (float or double).
+    template <class A> void fast_params(fastk::FastParams<A>& p) const;
+    bool uniform_inner() const { return unif_; }
+    const WorkItem* items_device() const { return items_.as<WorkItem>(); }
+    // host copy of the fast kernel's work items
+    std::vector<WorkItem> items_host() const;
     size_t lanczos_parts() const;  // partial sums written by apply_lanczos_f32
     static constexpr size_t kStageLimit = 200 * 1024;
 

@@ -21,7 +21,7 @@
 //   inner  - flips and conditions only on inner bits: the target lies in the
 //            same block, rank = block offset + inner_rank[b'];
 //   mixed  - everything else: full rank of the target.
-#include "ham.hpp"
+#include "fast_common.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -45,32 +45,9 @@ void DBuf::reset() {
 
 namespace {
 
-constexpr int kBlock = 256;
-constexpr uint32_t kChunk = 1024;
-constexpr int kMaxOuter = 256;
-constexpr int kMaxInnerTable = 512;  // inner terms a table may reference
-constexpr uint32_t kEllEmpty = 0xFFFFFFFFu;
+using namespace fastk;
+
 constexpr size_t kSmemTermBudget = 40 * 1024;
-
-template <class S, class A>
-struct alignas(16) KTerm {
-    S C, V, X, J;
-    A ar, ai;
-    uint32_t flags, var0;
-};
-template <class A>
-struct alignas(16) KVar {
-    uint64_t sm, pf;
-    A a0r, a0i, a1r, a1i;
-};
-
-template <class T> struct V2;
-template <> struct V2<double> { using t = double2; };
-template <> struct V2<float> { using t = float2; };
-
-template <class S> __device__ __forceinline__ int popcnt(S x);
-template <> __device__ __forceinline__ int popcnt<uint32_t>(uint32_t x) { return __popc(x); }
-template <> __device__ __forceinline__ int popcnt<uint64_t>(uint64_t x) { return __popcll(x); }
 
 template <class S>
 __device__ __forceinline__ bool in_basis(const DevBasis& b, S s) {
@@ -117,35 +94,6 @@ __device__ __forceinline__ S row_state(const DevBasis& b, const WorkItem& it, ui
         return (S)(((uint64_t)it.a << b.n_in) | (uint64_t)bb);
     }
     return (S)__ldg(reinterpret_cast<const unsigned long long*>(b.states_int) + it.row0 + r);
-}
-
-template <class S, class A>
-__device__ __forceinline__ void term_amp(const KTerm<S, A>& t, S s, const KVar<A>* __restrict__ vars, A& ar, A& ai) {
-    ar = t.ar;
-    ai = t.ai;
-    const uint32_t nv = (t.flags >> 8) & 0xffu;
-    for (uint32_t k = 0; k < nv; ++k) {
-        const KVar<A> v = vars[t.var0 + k];
-        const bool sel = (((uint64_t)s ^ v.pf) & v.sm) == v.sm;
-        const A cr = sel ? v.a1r : v.a0r, ci = sel ? v.a1i : v.a0i;
-        const A nr = ar * cr - ai * ci;
-        ai = ar * ci + ai * cr;
-        ar = nr;
-    }
-    if (popcnt<S>(s & t.J) & 1) {
-        ar = -ar;
-        ai = -ai;
-    }
-}
-
-template <class A, class X2>
-__device__ __forceinline__ void cmac(A& r, A& i, A ar, A ai, const X2& x, bool real) {
-    r = fma(ar, (A)x.x, r);
-    i = fma(ar, (A)x.y, i);
-    if (!real) {
-        r = fma(-ai, (A)x.y, r);
-        i = fma(ai, (A)x.x, i);
-    }
 }
 
 template <class S, class A>
@@ -312,80 +260,6 @@ __global__ void __launch_bounds__(kBlock) spmv_kernel(const SpmvParams<S, A> p, 
 // Jordan-Wigner sign folded in.  The table depends only on b, so one copy
 // serves every block.  Outer terms become a per-block list in shared memory;
 // the remaining (straddling) terms are evaluated generically.
-template <class A>
-struct alignas(16) OutEnt {
-    int32_t delta;
-    uint32_t J;
-    A ar, ai;
-};
-
-template <class A>
-struct FastParams {
-    int n_in;
-    uint32_t in_mask;
-    int ngroups, no_double, N;
-    uint32_t gmask0, gmask1;
-    int gpop0, gpop1;
-    const uint32_t* outer_off;
-    const uint32_t* inner_rank;   // null: inner rank = inner bits
-    const uint32_t* inner_state;  // null: inner configuration = table index
-    const WorkItem* items;
-    const uint32_t* iptr;         // table rows
-    const uint32_t* ient;         // entries: rank | inner sign << rbits | term << (rbits + 1)
-    int rbits;
-    const KTerm<uint32_t, A>* inner;  // per term: amplitude, J (its outer part signs per block)
-    int n_inner;
-    A u_ar, u_ai;                 // UNIF: the one amplitude (no signs)
-    const KTerm<uint32_t, A>* outer;
-    int n_outer, outer_has_j;
-    const KTerm<uint32_t, A>* mixed;
-    const KVar<A>* vars;
-    int n_mixed;
-    int diag_mode;
-    int n_dtab;
-    const void* dcode;
-    const A* dtab;
-    // Lanczos mode (all null otherwise): x = vtab[*kstep], y = vtab[*kstep + 1],
-    // y is scaled by sig[*kstep], and each block writes Re sum conj(x) y to apart.
-    const void* const* vtab;
-    const int* kstep;
-    const double* sig;
-    double2* apart;
-};
-
-// Compensated accumulation of a*b into (hi, lo) (TwoProduct + TwoSum).
-__device__ __forceinline__ void ffma_acc(float& hi, float& lo, float a, float b) {
-    const float p = a * b;
-    const float e = fmaf(a, b, -p);
-    const float t = hi + p;
-    const float z = t - hi;
-    lo += ((hi - (t - z)) + (p - z)) + e;
-    hi = t;
-}
-__device__ __forceinline__ void ffma_acc(double& hi, double& lo, double a, double b) { hi = fma(a, b, hi); }
-
-__device__ __forceinline__ double block_sum_d(double v) {
-    __shared__ double sh[32];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[wid] = v;
-    __syncthreads();
-    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : 0.0;
-    if (wid == 0)
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ bool in_basis_fast(int ng, uint32_t g0, uint32_t g1, int p0, int p1, int no_double, int N,
-                                              uint32_t s) {
-    if (ng > 0 && __popc(s & g0) != p0) return false;
-    if (ng > 1 && __popc(s & g1) != p1) return false;
-    if (no_double && (s & (s >> N) & ((1u << N) - 1u))) return false;
-    return true;
-}
-
-constexpr int kMaxMixedSmem = 64;
 // STAGE: the work item is a whole outer block and its x slice is staged in
 // shared memory, so inner-table gathers read shared memory.
 template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE>
@@ -1094,19 +968,11 @@ void Hamiltonian::autotune() {
     mode_ = saved;
 }
 
-template <class T, class A>
-static void launch_fast(const DevBasis& b, const DBuf& items, size_t n_items, const DBuf& iptr, const DBuf& ient,
-                        int rbits, bool unif, double uar, double uai, const DBuf& outer, int n_outer, int outer_has_j,
-                        const DBuf& inner, int n_inner, const DBuf& mixed, const DBuf& vars, int n_mixed, bool real,
-                        int diag_mode, const DBuf& dcode, const DBuf& dtab, const typename V2<T>::t* x,
-                        typename V2<T>::t* y, cudaStream_t s, FastVariant var, size_t stage_smem,
-                        const LanczosHooks* lz = nullptr) {
-    if (!n_items) return;
-    FastParams<A> p;
-    p.vtab = lz ? lz->vtab : nullptr;
-    p.kstep = lz ? lz->kstep : nullptr;
-    p.sig = lz ? lz->sig : nullptr;
-    p.apart = lz ? lz->apart : nullptr;
+template <class A>
+void Hamiltonian::fast_params(FastParams<A>& p) const {
+    const DevBasis& b = *db_;
+    const FastSet& fs = sizeof(A) == 8 ? f64s_ : f32s_;
+    std::memset(&p, 0, sizeof(p));
     p.n_in = b.n_in;
     p.in_mask = (uint32_t)b.in_mask;
     p.ngroups = b.ngroups;
@@ -1119,24 +985,41 @@ static void launch_fast(const DevBasis& b, const DBuf& items, size_t n_items, co
     p.outer_off = static_cast<const uint32_t*>(b.outer_off);
     p.inner_rank = b.inner_all ? nullptr : b.inner_rank;
     p.inner_state = b.inner_all ? nullptr : b.inner_state;
-    p.items = items.as<WorkItem>();
-    p.iptr = iptr.as<uint32_t>();
-    p.ient = ient.as<uint32_t>();
-    p.rbits = rbits;
-    p.inner = inner.as<KTerm<uint32_t, A>>();
-    p.n_inner = n_inner;
-    p.u_ar = (A)uar;
-    p.u_ai = (A)uai;
-    p.outer = outer.as<KTerm<uint32_t, A>>();
-    p.n_outer = n_outer;
-    p.outer_has_j = outer_has_j;
-    p.mixed = mixed.as<KTerm<uint32_t, A>>();
-    p.vars = vars.as<KVar<A>>();
-    p.n_mixed = n_mixed;
-    p.diag_mode = diag_mode;
+    p.items = items_.as<WorkItem>();
+    p.iptr = iptr_.as<uint32_t>();
+    p.ient = ient_.as<uint32_t>();
+    p.rbits = rbits_;
+    p.inner = fs.inner.as<KTerm<uint32_t, A>>();
+    p.n_inner = fs.n_inner;
+    p.u_ar = (A)u_ar_;
+    p.u_ai = (A)u_ai_;
+    p.outer = fs.outer.as<KTerm<uint32_t, A>>();
+    p.n_outer = fs.n_outer;
+    p.outer_has_j = fs.outer_has_j;
+    p.mixed = fs.mixed.as<KTerm<uint32_t, A>>();
+    p.vars = fs.vars.as<KVar<A>>();
+    p.n_mixed = fs.n_mixed;
+    p.diag_mode = diag_mode_;
+    const DBuf& dtab = sizeof(A) == 8 ? dtab64_ : dtab32_;
     p.n_dtab = (int)(dtab.bytes / (2 * sizeof(A)));
-    p.dcode = dcode.p;
+    p.dcode = dcode_.p;
     p.dtab = dtab.as<A>();
+}
+template void Hamiltonian::fast_params<float>(FastParams<float>&) const;
+std::vector<WorkItem> Hamiltonian::items_host() const {
+    std::vector<WorkItem> v(n_items_);
+    if (n_items_) QKG_CUDA(cudaMemcpy(v.data(), items_.p, n_items_ * sizeof(WorkItem), cudaMemcpyDeviceToHost));
+    return v;
+}
+template void Hamiltonian::fast_params<double>(FastParams<double>&) const;
+
+// Launch the fast kernel in variant var; p.items must list the variant's work
+// items (one per outer block for the staged variant).
+template <class T, class A>
+static void launch_fast(const FastParams<A>& p, size_t n_items, bool real, bool unif, const typename V2<T>::t* x,
+                        typename V2<T>::t* y, cudaStream_t s, FastVariant var, size_t stage_smem) {
+    if (!n_items) return;
+    const int outer_has_j = p.outer_has_j;
     const unsigned g = (unsigned)n_items;
     const int key = (var == FV_STAGED ? 8 : 0) | (real ? 4 : 0) | (unif ? 2 : 0) | (outer_has_j ? 1 : 0);
     const size_t sm = stage_smem;
@@ -1304,10 +1187,11 @@ void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const 
     if (fast()) {
         const FastVariant v = variant(16);
         const bool st = v == FV_STAGED;
-        launch_fast<double, double>(*db_, st ? items_blk_ : items_, st ? n_items_blk_ : n_items_, iptr_, ient_, rbits_,
-                                    unif_, u_ar_, u_ai_, f64s_.outer, f64s_.n_outer, f64s_.outer_has_j, f64s_.inner,
-                                    f64s_.n_inner, f64s_.mixed, f64s_.vars, f64s_.n_mixed, all_real_, diag_mode_,
-                                    dcode_, dtab64_, x, y, s, v, st ? max_block_ * 16 : 0);
+        FastParams<double> p;
+        fast_params(p);
+        if (st) p.items = items_blk_.as<WorkItem>();
+        launch_fast<double, double>(p, st ? n_items_blk_ : n_items_, all_real_, unif_, x, y, s, v,
+                                    st ? max_block_ * 16 : 0);
         return;
     }
     const DBuf& full = dfull64_;
@@ -1321,10 +1205,15 @@ void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) cons
     QKG_REQUIRE(fast(), "the device-resident Lanczos step needs the fast SpMV kernel");
     const FastVariant v = variant(8);
     const bool st = v == FV_STAGED;
-    launch_fast<float, float>(*db_, st ? items_blk_ : items_, st ? n_items_blk_ : n_items_, iptr_, ient_, rbits_, unif_,
-                              u_ar_, u_ai_, f32s_.outer, f32s_.n_outer, f32s_.outer_has_j, f32s_.inner, f32s_.n_inner,
-                              f32s_.mixed, f32s_.vars, f32s_.n_mixed, all_real_, diag_mode_, dcode_, dtab32_, nullptr,
-                              nullptr, s, v, st ? max_block_ * 8 : 0, &lz);
+    FastParams<float> p;
+    fast_params(p);
+    if (st) p.items = items_blk_.as<WorkItem>();
+    p.vtab = lz.vtab;
+    p.kstep = lz.kstep;
+    p.sig = lz.sig;
+    p.apart = lz.apart;
+    launch_fast<float, float>(p, st ? n_items_blk_ : n_items_, all_real_, unif_, nullptr, nullptr, s, v,
+                              st ? max_block_ * 8 : 0);
 }
 
 size_t Hamiltonian::lanczos_parts() const { return staged(8) ? n_items_blk_ : n_items_; }
@@ -1333,10 +1222,11 @@ void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
     if (fast()) {
         const FastVariant v = variant(8);
         const bool st = v == FV_STAGED;
-        launch_fast<float, float>(*db_, st ? items_blk_ : items_, st ? n_items_blk_ : n_items_, iptr_, ient_, rbits_,
-                                  unif_, u_ar_, u_ai_, f32s_.outer, f32s_.n_outer, f32s_.outer_has_j, f32s_.inner,
-                                  f32s_.n_inner, f32s_.mixed, f32s_.vars, f32s_.n_mixed, all_real_, diag_mode_, dcode_,
-                                  dtab32_, x, y, s, v, st ? max_block_ * 8 : 0);
+        FastParams<float> p;
+        fast_params(p);
+        if (st) p.items = items_blk_.as<WorkItem>();
+        launch_fast<float, float>(p, st ? n_items_blk_ : n_items_, all_real_, unif_, x, y, s, v,
+                                  st ? max_block_ * 8 : 0);
         return;
     }
     if (wide_)

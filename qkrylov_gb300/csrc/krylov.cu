@@ -15,7 +15,7 @@
 // thread's partial sum is as accurate as if computed in twice the working
 // precision.  Partials are then combined in FP64.  This keeps the reductions
 // off GB300's low-rate FP64 pipe.
-#include "ham.hpp"
+#include "fast_common.cuh"
 
 #include <algorithm>
 
@@ -286,48 +286,12 @@ __global__ void precond_kernel(const double2* __restrict__ r, const double2* __r
     }
 }
 
-// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw, "Parallel
-// random numbers: as easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64-bit
-// multiplies with the round keys bumped by the Weyl constants.
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-        const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
-        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-        k.x += W0;
-        k.y += W1;
-    }
-    return c;
-}
 // Element i gets one Philox block; Box-Muller turns its words into a complex
 // standard normal (real and imaginary parts independent N(0,1)).
 template <class T2, bool F64>
 __global__ void philox_normal_kernel(uint64_t seed, uint64_t stream, T2* out, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint4 r = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), (uint32_t)stream, (uint32_t)(stream >> 32)),
-                                      make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
-        T2 o;
-        if (F64) {
-            const double u1 = ((double)r.x + 1.0) * 2.3283064365386963e-10;  // (0, 1]
-            const double u2 = (double)r.y * 2.3283064365386963e-10;
-            const double rad = sqrt(-2.0 * log(u1));
-            double sn, cs;
-            sincospi(2.0 * u2, &sn, &cs);
-            o.x = rad * cs;
-            o.y = rad * sn;
-        } else {
-            const float u1 = ((float)r.x + 1.0f) * 2.3283064e-10f;
-            const float u2 = (float)r.y * 2.3283064e-10f;
-            const float rad = sqrtf(-2.0f * logf(u1));
-            float sn, cs;
-            sincospif(2.0f * u2, &sn, &cs);
-            o.x = rad * cs;
-            o.y = rad * sn;
-        }
-        out[i] = o;
-    }
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = fastk::philox_cnormal<T2, F64>(seed, stream, i);
 }
 
 double2* finish(Workspace& ws, int nparts, int stride, int k, cudaStream_t s) {

@@ -269,9 +269,11 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     auto capture = [&](bool so) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
+        const uint64_t c0 = launch_count();
         QKG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         enqueue_step(so, nullptr);
         QKG_CUDA(cudaStreamEndCapture(st, &g));
+        add_launches(-(int64_t)(launch_count() - c0));
         QKG_CUDA(cudaGraphInstantiate(&ge, g, 0));
         QKG_CUDA(cudaGraphDestroy(g));
         return ge;

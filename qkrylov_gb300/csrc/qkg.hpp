@@ -38,6 +38,9 @@ const char* last_error();
 // (qkrylov_kernel_launches()) and surfaces launch errors.
 void count_launch();
 uint64_t launch_count();
+// Graph capture records launches without running them: the capturing code
+// takes them back (negative d) and adds the graph's kernels per replay.
+void add_launches(int64_t d);
 #define QKG_LAUNCHED()               \
     do {                             \
         ::qkg::count_launch();       \

@@ -256,29 +256,6 @@ void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, 
 }
 
 // ============================================================ random streams
-namespace {
-template <class Dist>
-void fill_stream(std::mt19937& rng, Dist& dist, uint64_t n, cd* out) {
-    for (uint64_t i = 0; i < n; ++i) {
-        const double im = dist(rng);  // g++ evaluates the imaginary argument first
-        const double re = dist(rng);
-        out[i] = cd(re, im);
-    }
-}
-// One random stream across all vectors (src/solvers/ftlm.cpp:133-143).
-struct NormalStream {
-    std::mt19937 rng{42};
-    std::normal_distribution<double> d64{0.0, 1.0};
-    std::normal_distribution<float> d32{0.0f, 1.0f};
-    bool f32;
-    explicit NormalStream(bool f) : f32(f) {}
-    void fill(uint64_t n, cd* out) {
-        if (f32) fill_stream(rng, d32, n, out);
-        else fill_stream(rng, d64, n, out);
-    }
-};
-}  // namespace
-
 void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out, bool f32) {
     std::mt19937 rng(seed);
     if (f32) {

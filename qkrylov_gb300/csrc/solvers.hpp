@@ -4,6 +4,7 @@
 #include "ham.hpp"
 
 #include <complex>
+#include <random>
 #include <vector>
 
 namespace qkg {
@@ -32,6 +33,27 @@ void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, 
 // `f32` draws through the float distributions, as the reference's FP32 engine
 // (the one behind its C API, where Real = float) does.
 void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out, bool f32 = false);
+template <class Dist>
+void fill_stream(std::mt19937& rng, Dist& dist, uint64_t n, cd* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        const double im = dist(rng);  // g++ evaluates the imaginary argument first
+        const double re = dist(rng);
+        out[i] = cd(re, im);
+    }
+}
+// The FTLM random stream: one mt19937(42) normal stream across all vectors of
+// one run (src/solvers/ftlm.cpp:133-143).
+struct NormalStream {
+    std::mt19937 rng{42};
+    std::normal_distribution<double> d64{0.0, 1.0};
+    std::normal_distribution<float> d32{0.0f, 1.0f};
+    bool f32;
+    explicit NormalStream(bool f) : f32(f) {}
+    void fill(uint64_t n, cd* out) {
+        if (f32) fill_stream(rng, d32, n, out);
+        else fill_stream(rng, d64, n, out);
+    }
+};
 // Device Philox4x32-10 (Salmon et al., SC'11) Gaussian complex vectors.
 void philox_normal_f64(uint64_t seed, uint64_t stream, double2* out, uint64_t n, cudaStream_t s);
 void philox_normal_f32(uint64_t seed, uint64_t stream, float2* out, uint64_t n, cudaStream_t s);

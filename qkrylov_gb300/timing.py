@@ -1,0 +1,67 @@
+"""Time the SpMV kernel on a chain model (also the command the kernel
+profiles are taken with).
+
+    python -m qkrylov_gb300.timing --model heisenberg --L 28 --precision fp32 --mode 0 --reps 5
+
+Builds the Hamiltonian (Heisenberg chain ``Sz Sz + 0.5 (S+ S- + S- S+)`` per
+bond, or Fermi-Hubbard chain ``-t c^dag c`` hopping per spin and direction plus
+``U n_up n_dn``), periodic unless ``--obc``, in the Sz = 0 / half-filled
+sector, then times ``reps`` back-to-back applies on internal device vectors
+with CUDA events on the Hamiltonian's stream.  Prints one JSON line with the
+mean launch time and the algorithmic bandwidth (read x once, write y once).
+"""
+import argparse
+import json
+import time
+
+import qkrylov_gb300 as qk
+
+
+def heisenberg_chain(L, pbc=True, J=1.0):
+    ops = qk.OpSum()
+    for i in range(L if pbc else L - 1):
+        j = (i + 1) % L
+        ops.add_term(J, "Sz", i, "Sz", j)
+        ops.add_term(0.5 * J, "Sp", i, "Sm", j)
+        ops.add_term(0.5 * J, "Sm", i, "Sp", j)
+    return qk.SpinHalfBasis(L, conserve_sz=True, sz=0), qk.SpinHalfSite(), ops
+
+
+def hubbard_chain(L, pbc=True, t=1.0, U=4.0):
+    ops = qk.OpSum()
+    for i in range(L if pbc else L - 1):
+        j = (i + 1) % L
+        for s in ("Up", "Dn"):
+            ops.add_term(-t, "Cdag" + s, i, "C" + s, j)
+            ops.add_term(-t, "Cdag" + s, j, "C" + s, i)
+    for i in range(L):
+        ops.add_term(U, "Nupdn", i)
+    return qk.HubbardBasis(L, nup=L // 2, ndn=L // 2), qk.HubbardSite(), ops
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--model", choices=["heisenberg", "hubbard"], default="heisenberg")
+    p.add_argument("--L", type=int, default=28)
+    p.add_argument("--obc", action="store_true")
+    p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    p.add_argument("--mode", type=int, default=0, help="0 autotuned, 1 generic, 2 fast, 3 fast staged, 4 fast rows4")
+    p.add_argument("--reps", type=int, default=5)
+    a = p.parse_args()
+    build = heisenberg_chain if a.model == "heisenberg" else hubbard_chain
+    basis, site, ops = build(a.L, not a.obc)
+    t0 = time.perf_counter()
+    H = qk.MatrixFreeHamiltonian(basis, site, ops)
+    tc = time.perf_counter() - t0
+    fast = H.select_kernel(mode=a.mode)
+    fp32 = a.precision == "fp32"
+    ms = H.benchmark_apply(fp32=fp32, reps=a.reps)
+    n = H.dimension
+    e = 8 if fp32 else 16
+    print(json.dumps({"model": a.model, "L": a.L, "pbc": not a.obc, "dim": n, "precision": a.precision,
+                      "mode": a.mode, "fast": fast, "ms": ms, "alg_GBs": 2 * n * e / ms / 1e6,
+                      "construct_s": round(tc, 3)}), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+"""Batched (block-vector) Lanczos: FTLM over all Sz sectors in one run and
+continued fractions for several right-hand sides, against the oracle's
+single-vector restatement of ftlm.cpp / dynamics.cpp."""
+import numpy as np
+import pytest
+
+import models as M
+from conftest import make_model
+from oracle_ctypes import OHam, spectral
+
+pytestmark = pytest.mark.gpu
+
+EARLY_RTOL = 1e-10   # FP64 alphas/betas of the first steps (before loss of orthogonality amplifies rounding)
+OBS_RTOL = 1e-8      # FP64 Z, E, Cv and S(omega)
+MIXED_RTOL = 1e-4    # FP32 vectors / FP64 reductions against FP64
+
+
+def chain_sectors(qk, L, pbc=True):
+    hams, models = [], []
+    for sz2 in range(-L, L + 1, 2):
+        sec = M.sector(sz2=sz2)
+        terms = M.heisenberg_terms(L, pbc)
+        b, s, o = make_model(qk, M.SPIN, L, sec, terms)
+        hams.append(qk.MatrixFreeHamiltonian(b, s, o))
+        models.append((M.SPIN, L, sec, terms))
+    return hams, models
+
+
+def combine(parts, betas):
+    """Sum of per-sector FTLM estimates (Z_s, E_s, Cv_s) into the ensemble's."""
+    Z = sum(p[0] for p in parts)
+    E = sum(p[0] * p[1] for p in parts) / Z
+    E2 = sum(p[0] * (p[2] / betas ** 2 + p[1] ** 2) for p in parts) / Z
+    return Z, E, betas ** 2 * (E2 - E ** 2)
+
+
+def test_block_fp64_tridiagonals_match_oracle(qk, oracle):
+    L, R, Mst = 10, 3, 15
+    hams, models = chain_sectors(qk, L)
+    res = qk.block_lanczos_tridiag(hams, R, Mst, mixed=False, start="ftlm")
+    assert res.stats["padded_vectors"] == 4
+    for h, m in enumerate(models):
+        a, b, na, nb, nr = OHam(oracle, *m).ftlm_tridiag(R, Mst)
+        for v in range(R):
+            i = h * R + v
+            np.testing.assert_allclose(res.norm2[i], nr[v] ** 2, rtol=1e-12)
+            ga, gb = res.alphas[i], res.betas[i]
+            scale = max(1.0, np.abs(a[v, :na[v]]).max())
+            # steps before the Krylov space closes (beta at rounding level, where
+            # the 1e-15 stop decides on noise): they must agree
+            ob = b[v, :nb[v]]
+            closed = np.nonzero(ob < 1e-8 * scale)[0]
+            kb = min(8, len(gb), int(closed[0]) if closed.size else nb[v])
+            k = min(kb + 1, na[v], len(ga))
+            assert k >= 1
+            assert np.abs(ga[:k] - a[v, :k]).max() <= EARLY_RTOL * scale
+            if kb:
+                assert np.abs(gb[:kb] - ob[:kb]).max() <= EARLY_RTOL * scale
+            if not closed.size and hams[h].dimension > Mst:
+                assert len(ga) == na[v] and len(gb) == nb[v]
+
+
+def test_block_sector_batch_equals_single(qk):
+    hams, _ = chain_sectors(qk, 12)
+    both = qk.block_lanczos_tridiag([hams[5], hams[6]], 4, 20, mixed=True, start="philox", seed=9)
+    one = qk.block_lanczos_tridiag([hams[5]], 4, 20, mixed=True, start="philox", seed=9)
+    for v in range(4):
+        np.testing.assert_array_equal(both.alphas[v], one.alphas[v])
+        np.testing.assert_array_equal(both.betas[v], one.betas[v])
+
+
+def test_block_philox_deterministic(qk):
+    hams, _ = chain_sectors(qk, 12)
+    r1 = qk.block_lanczos_tridiag(hams, 8, 12, mixed=True, start="philox", seed=5)
+    r2 = qk.block_lanczos_tridiag(hams, 8, 12, mixed=True, start="philox", seed=5)
+    r3 = qk.block_lanczos_tridiag(hams, 8, 12, mixed=True, start="philox", seed=6)
+    for i in range(len(r1.alphas)):
+        np.testing.assert_array_equal(r1.alphas[i], r2.alphas[i])
+    mid = len(hams) // 2 * 8
+    assert not np.array_equal(r1.alphas[mid], r3.alphas[mid])
+    # Gaussian complex start vectors: E|x|^2 = 2 per component
+    dims = np.repeat([h.dimension for h in hams], 8)
+    big = dims >= 500
+    assert np.all(np.abs(r1.norm2[big] / (2 * dims[big]) - 1) < 0.2)
+
+
+def test_ftlm_sectors_fp64_matches_oracle(qk, oracle):
+    L, R, Mst = 10, 4, 20
+    betas = np.array([0.1, 0.5, 1.0, 3.0])
+    hams, models = chain_sectors(qk, L)
+    r = qk.ftlm_sectors(hams, betas, n_random=R, n_steps=Mst, mixed=False, start="ftlm")
+    parts = []
+    for m in models:
+        o = OHam(oracle, *m)
+        z = np.array([o.ftlm(b, R, Mst) for b in betas])
+        parts.append((z[:, 0], z[:, 1], z[:, 2]))
+    Z, E, C = combine(parts, betas)
+    np.testing.assert_allclose(r.partition_function, Z, rtol=OBS_RTOL)
+    np.testing.assert_allclose(r.internal_energy, E, rtol=OBS_RTOL, atol=OBS_RTOL)
+    np.testing.assert_allclose(r.specific_heat, C, rtol=OBS_RTOL, atol=OBS_RTOL)
+    s = qk.ftlm_sectors(hams, betas, n_random=R, n_steps=Mst, mixed=False, start="ftlm", shifted=True)
+    np.testing.assert_allclose(s.partition_function * np.exp(s.log_shift), Z, rtol=OBS_RTOL)
+    np.testing.assert_allclose(s.specific_heat, C, rtol=OBS_RTOL, atol=OBS_RTOL)
+
+
+def test_ftlm_sectors_mixed_vs_fp64(qk):
+    L, R, Mst = 14, 8, 40
+    betas = np.geomspace(0.1, 10.0, 7)
+    hams, _ = chain_sectors(qk, L)
+    r64 = qk.ftlm_sectors(hams, betas, n_random=R, n_steps=Mst, mixed=False, start="ftlm", shifted=True)
+    r32 = qk.ftlm_sectors(hams, betas, n_random=R, n_steps=Mst, mixed=True, start="ftlm", shifted=True)
+    z64 = r64.partition_function * np.exp(r64.log_shift - r64.log_shift)
+    z32 = r32.partition_function * np.exp(r32.log_shift - r64.log_shift)
+    np.testing.assert_allclose(z32, z64, rtol=MIXED_RTOL)
+    np.testing.assert_allclose(r32.internal_energy, r64.internal_energy, rtol=MIXED_RTOL, atol=MIXED_RTOL)
+    np.testing.assert_allclose(r32.specific_heat, r64.specific_heat, rtol=MIXED_RTOL, atol=MIXED_RTOL)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_cf_block_matches_oracle(qk, oracle, mixed):
+    # Hubbard chain: a permuted basis, so the start vectors go through the
+    # reference-to-internal permutation
+    L, n_iter = 6, 30
+    m = (M.HUBBARD, L, M.sector(nup=3, ndn=3), M.hubbard_terms(L, True))
+    b, s, o = make_model(qk, *m)
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    n = H.dimension
+    rng = np.random.default_rng(3)
+    phis = rng.normal(size=(5, n)) + 1j * rng.normal(size=(5, n))
+    phis[2] = 0.0  # a zero right-hand side gets no coefficients (dynamics.cpp:27)
+    res, stats = qk.continued_fraction_block(H, phis, n_iter=n_iter, mixed=mixed)
+    assert stats["padded_vectors"] == 8
+    oh = OHam(oracle, *m)
+    omegas = np.linspace(-2.0, 8.0, 41)
+    for i in range(5):
+        a, bb, nrm = oh.cf(phis[i], n_iter)
+        if i == 2:
+            assert res[i].norm_phi0 == 0.0 and len(res[i].alphas) == 0
+            continue
+        np.testing.assert_allclose(res[i].norm_phi0, nrm, rtol=1e-12 if not mixed else 1e-6)
+        assert len(res[i].alphas) == len(a) and len(res[i].betas) == len(bb)
+        if not mixed:
+            k = min(10, len(a))
+            assert np.abs(res[i].alphas[:k] - a[:k]).max() <= EARLY_RTOL * max(1.0, np.abs(a).max())
+        S = np.array([qk.evaluate_spectral_function(res[i], w, -3.0, eta=0.2) for w in omegas])
+        So = np.array([spectral(oracle, a, bb, nrm, w, -3.0, 0.2) for w in omegas])
+        tol = OBS_RTOL if not mixed else MIXED_RTOL
+        assert np.abs(S - So).max() <= tol * np.abs(So).max()
+
+
+def test_block_rejects_bad_arguments(qk):
+    hams, _ = chain_sectors(qk, 6)
+    with pytest.raises(qk.QKrylovError):
+        qk.block_lanczos_tridiag(hams, 33, 4)
+    with pytest.raises(qk.QKrylovError):
+        qk.ftlm_sectors(hams, [1.0], n_random=0)
