@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-ftlm", action="store_true", help="skip the batched FTLM measurement")
     p.add_argument("--cpu-sample-rows", type=int, default=1 << 19)
     return p.parse_args()
 
@@ -281,7 +282,10 @@ def main():
     alg_bytes = 2 * DIM * BYTES_PER_ELEM_F32
     achieved = alg_bytes / spmv_s / 1e9
     tr = profile_traffic()
-    out["roofline"] = {"kernel": "spmv_kernel<uint32,float> (FP32 SpMV)", "bound": "hbm", "achieved": achieved,
+    variant, _ = H.tuning(fp32=True)
+    kname = {"rows4": "spmv_rows_kernel<float>", "row": "spmv_fast_kernel<float>",
+             "staged": "spmv_fast_kernel<float, staged>"}.get(variant, "spmv_kernel<float>")
+    out["roofline"] = {"kernel": kname + " (FP32 SpMV)", "bound": "hbm", "achieved": achieved,
                        "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
                        "traffic": tr, "algorithmic_bytes_per_launch": alg_bytes,
                        "launch_ms": spmv_s * 1e3}
@@ -300,9 +304,59 @@ def main():
                        "spmv_ms": 1e3 * r64.seconds_spmv / max(1, r64.spmv_calls),
                        "form": "reference semantics: FP64 vectors and SpMV, full reorthogonalisation"}
         out["dE0_vs_fp64"] = {"abs": de, "rel": de / abs(r64.energy), "meets_1e-10": de <= 1e-10 * abs(r64.energy)}
+    if not args.no_ftlm:
+        out["ftlm"] = ftlm_batch(qk, args.seed, hbm_peak, peak_kind)
     if ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_sample_rows, os.cpu_count() or 1)
     print(json.dumps(out), flush=True)
+
+
+FTLM_L, FTLM_R, FTLM_M, FTLM_NT = 24, 32, 100, 200
+
+
+def ftlm_batch(qk, seed, hbm_peak, peak_kind):
+    """Batched FTLM: Heisenberg chain L=24 periodic, all 25 Sz sectors, 32
+    Philox Gaussian vectors per sector, 100 Lanczos steps each, one block SpMV
+    launch per step for all 800 vectors; Z, E, Cv at 200 log-spaced T in
+    [0.01, 10] (shifted evaluation).  Mixed form (FP32 block vectors and SpMV,
+    compensated reductions in FP64) and the FP64 form on the same vectors."""
+    import models as M
+    from conftest import make_model
+    hams = []
+    for sz2 in range(-FTLM_L, FTLM_L + 1, 2):
+        b, s, o = make_model(qk, M.SPIN, FTLM_L, M.sector(sz2=sz2), M.heisenberg_terms(FTLM_L, True))
+        hams.append(qk.MatrixFreeHamiltonian(b, s, o))
+    betas = 1.0 / np.geomspace(0.01, 10.0, FTLM_NT)
+    qk.ftlm_sectors(hams, betas, n_random=FTLM_R, n_steps=3, mixed=True, start="philox", seed=seed)  # warm-up
+    res = {}
+    for mixed in (True, False):
+        t0 = time.perf_counter()
+        r = qk.ftlm_sectors(hams, betas, n_random=FTLM_R, n_steps=FTLM_M, mixed=mixed, start="philox", seed=seed,
+                            shifted=True)
+        wall = time.perf_counter() - t0
+        res[mixed] = (r, wall)
+    r32, w32 = res[True]
+    r64, w64 = res[False]
+    st = r32.stats
+    nvec = FTLM_R * len(hams)
+    e = 8
+    alg = 2 * st["rows"] * st["padded_vectors"] * e
+    achieved = alg / (st["spmv_ms"] * 1e-3) / 1e9
+    fin = np.isfinite(r64.internal_energy) & np.isfinite(r32.internal_energy)
+    dE = np.abs(r32.internal_energy - r64.internal_energy)[fin]
+    dC = np.abs(r32.specific_heat - r64.specific_heat)[fin]
+    return {"workload": f"heisenberg_chain_L{FTLM_L}_pbc_all_{len(hams)}_sz_sectors_R{FTLM_R}_M{FTLM_M}_T{FTLM_NT}",
+            "rows": st["rows"], "vectors": nvec, "vectors_per_s": nvec / st["seconds"],
+            "e2e_vectors_per_s": nvec / w32, "loop_s": st["seconds"],
+            "fp64_vectors_per_s": nvec / r64.stats["seconds"], "fp64_loop_s": r64.stats["seconds"],
+            "tile": {"vectors_per_lane": st["vectors_per_lane"], "tune_ms": st["tune_ms"]},
+            "roofline": {"kernel": "spmv_block_kernel<float> (FP32 block SpMV, 32 vectors)", "bound": "hbm",
+                         "achieved": achieved, "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "algorithmic_bytes_per_launch": alg,
+                         "launch_ms": st["spmv_ms"]},
+            "mixed_vs_fp64": {"max_abs_dE": float(dE.max()) if dE.size else None,
+                              "max_abs_dCv": float(dC.max()) if dC.size else None},
+            "start_vectors": "seeded Philox Gaussian (device)"}
 
 
 def _cudart():

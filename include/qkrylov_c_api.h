@@ -276,6 +276,13 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* n_outer, int* n_inner
  * (optional) reports whether the fast kernel applies. */
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use);
 
+/* The fast-kernel variant mode 0 uses for FP32 (fp32 != 0) or FP64 vectors
+ * (*variant: 0 one row per thread, 1 staged, 2 four rows per thread; -1 when
+ * the generic kernel applies) and the autotuner's mean launch times per
+ * variant (ms_per_variant[3], 0 = not measured; sectors below 2^20 rows are
+ * not timed). */
+int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, double* ms_per_variant);
+
 /* Time `reps` back-to-back applies of the FP32 (fp32 != 0) or FP64 kernel on
  * internal device vectors, with CUDA events on the Hamiltonian's stream;
  * *ms_per_apply receives the mean launch duration. */
@@ -316,9 +323,11 @@ typedef struct {
  * steps each.  start_vectors (QKRYLOV_START_GIVEN): for each Hamiltonian in
  * order, n_vec vectors of its dimension, complex interleaved [re, im].
  * alphas/betas: [i * n_steps + k]; n_alpha/n_beta: counts recorded per vector;
- * norm2: squared norm of each start vector.  stats is optional. */
+ * norm2: squared norm of each start vector.  vectors_per_lane: block-SpMV
+ * tile (1, 2 or 4 vectors per lane; 0 = autotuned).  stats is optional. */
 int qkrylov_block_lanczos_tridiag(const qkrylov_hamiltonian_h* hams, int n_ham, int n_vec, int n_steps, int mixed,
-                                  int start_kind, uint64_t seed, const double* start_vectors, double* alphas,
+                                  int vectors_per_lane, int start_kind, uint64_t seed, const double* start_vectors,
+                                  double* alphas,
                                   double* betas, int* n_alpha, int* n_beta, double* norm2,
                                   qkrylov_block_stats_t* stats);
 

@@ -16,7 +16,7 @@ import os as _os
 import numpy as _np
 
 _HERE = _os.path.dirname(_os.path.abspath(__file__))
-LIB_PATH = _os.path.join(_HERE, "_lib", "libqkrylov_gb300.so")
+LIB_PATH = _os.environ.get("QKRYLOV_GB300_LIB") or _os.path.join(_HERE, "_lib", "libqkrylov_gb300.so")
 
 SUCCESS, ERROR_INVALID_ARG, ERROR_EXCEPTION, ERROR_CUDA, ERROR_DEVICE_TIMEOUT = 0, -1, -2, -3, -4
 
@@ -56,7 +56,7 @@ START_FTLM_STREAM, START_PHILOX, START_GIVEN, START_FTLM_STREAM_F32 = 0, 1, 2, 3
 # name: (restype, argtypes)
 _SIGS = {
     "qkrylov_last_error": (_c.c_char_p, []),
-    "qkrylov_block_lanczos_tridiag": (_i, [_vp, _i, _i, _i, _i, _i, _u64, _dp, _dp, _dp, _ip, _ip, _dp, _vp]),
+    "qkrylov_block_lanczos_tridiag": (_i, [_vp, _i, _i, _i, _i, _i, _i, _u64, _dp, _dp, _dp, _ip, _ip, _dp, _vp]),
     "qkrylov_ftlm_sectors_f64": (_i, [_vp, _i, _dp, _i, _i, _i, _i, _i, _u64, _dp, _dp, _dp, _dp, _vp]),
     "qkrylov_cf_block_f64": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, _ip, _ip, _dp, _vp]),
     "qkrylov_sector_create": (_vp, []),
@@ -127,6 +127,7 @@ _SIGS = {
     "qkrylov_hamiltonian_info": (_i, [_vp, _ip, _ip, _ip, _ip, _ip]),
     "qkrylov_hamiltonian_entries": (_i, [_vp, _u64p, _u64p, _u64p, _dp]),
     "qkrylov_hamiltonian_select_kernel": (_i, [_vp, _i, _ip]),
+    "qkrylov_hamiltonian_tuning": (_i, [_vp, _i, _ip, _dp]),
     "qkrylov_hamiltonian_benchmark_apply": (_i, [_vp, _i, _i, _dp]),
 }
 
@@ -371,6 +372,15 @@ class MatrixFreeHamiltonian(_Handle):
         _check(lib().qkrylov_hamiltonian_select_kernel(self._h, m, _c.byref(f)))
         return bool(f.value)
 
+    def tuning(self, fp32=True):
+        """(variant, {variant: autotuned ms}) of the fast kernel used in mode 0;
+        variant names: "row", "staged", "rows4" ("generic" when it does not apply)."""
+        v = _c.c_int()
+        ms = (_c.c_double * 3)()
+        _check(lib().qkrylov_hamiltonian_tuning(self._h, int(bool(fp32)), _c.byref(v), ms))
+        names = ["row", "staged", "rows4"]
+        return ("generic" if v.value < 0 else names[v.value]), {names[i]: ms[i] for i in range(3)}
+
     def benchmark_apply(self, fp32=True, reps=10):
         """Mean CUDA-event duration (ms) of one apply of the selected kernel."""
         ms = _c.c_double()
@@ -547,13 +557,14 @@ class BlockTridiagResult:
         self.alphas, self.betas, self.norm2, self.stats = alphas, betas, norm2, stats
 
 
-def block_lanczos_tridiag(hams, n_vec, n_steps, mixed=True, start="ftlm", seed=0, start_vectors=None):
+def block_lanczos_tridiag(hams, n_vec, n_steps, mixed=True, start="ftlm", seed=0, start_vectors=None, vpl=0):
     """Three-term Lanczos (no reorthogonalisation, stop at beta < 1e-15) of
     n_vec vectors for each Hamiltonian in ``hams``, all advanced together by
     one block-SpMV launch per step.  ``start``: "ftlm" (the reference FTLM
     stream, mt19937(42) per Hamiltonian), "ftlm32" (its float variant),
     "philox" (device Gaussian vectors from ``seed``) or "given"
-    (``start_vectors``: per Hamiltonian an (n_vec, dim) complex array)."""
+    (``start_vectors``: per Hamiltonian an (n_vec, dim) complex array).
+    ``vpl``: block-SpMV vectors per lane (1, 2, 4; 0 = autotuned)."""
     hams, arr = _ham_array(hams)
     kind = _STARTS[start]
     buf = None
@@ -570,7 +581,7 @@ def block_lanczos_tridiag(hams, n_vec, n_steps, mixed=True, start="ftlm", seed=0
     nb = _np.zeros(nv, dtype=_np.int32)
     n2 = _np.zeros(nv)
     st = BlockStatsC()
-    _check(lib().qkrylov_block_lanczos_tridiag(arr, len(hams), int(n_vec), int(n_steps), int(bool(mixed)), kind,
+    _check(lib().qkrylov_block_lanczos_tridiag(arr, len(hams), int(n_vec), int(n_steps), int(bool(mixed)), int(vpl), kind,
                                                int(seed), _dptr(buf.view(_np.float64)) if buf is not None else None,
                                                _dptr(a), _dptr(b), na.ctypes.data_as(_ip), nb.ctypes.data_as(_ip),
                                                _dptr(n2), _c.byref(st)))

@@ -76,8 +76,18 @@ __device__ __forceinline__ void vstore(typename V2<T>::t* p, const typename V2<T
 
 // y = diag(scale) H x for the Rp vectors of every Hamiltonian; with apart,
 // CTA c writes Re sum conj(x_v) y_v over its rows to apart[c * Rp + v].
+// Resident CTAs per SM the register allocation is held to (FP32 / FP64).
+#ifndef QKG_BLOCK_MINB
+#define QKG_BLOCK_MINB 4
+#endif
+#ifndef QKG_BLOCK_MINB64
+#define QKG_BLOCK_MINB64 2
+#endif
+#ifndef QKG_BLOCK_PREFETCH
+#define QKG_BLOCK_PREFETCH 1
+#endif
 template <class T, class A, bool REAL, bool UNIF, bool OJ, int VPL>
-__global__ void __launch_bounds__(kBlock) spmv_block_kernel(const FastParams<A>* __restrict__ P,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_BLOCK_MINB : QKG_BLOCK_MINB64) spmv_block_kernel(const FastParams<A>* __restrict__ P,
                                                             const BItem* __restrict__ items, int Rp,
                                                             const typename V2<T>::t* __restrict__ X,
                                                             typename V2<T>::t* __restrict__ Y,
@@ -194,10 +204,20 @@ __global__ void __launch_bounds__(kBlock) spmv_block_kernel(const FastParams<A>*
         }
         const uint32_t grp = it.pad + (r >> 5);
         const uint32_t e0 = __ldg(iptr + grp) + (r & 31u), e1 = __ldg(iptr + grp + 1);
+#if QKG_BLOCK_PREFETCH
+        // the next entry is loaded while this entry's gather is in flight
+        uint32_t nxt = e0 < e1 ? __ldg(ient + e0) : kEllEmpty;
+        for (uint32_t e = e0; nxt != kEllEmpty;) {
+            const uint32_t ent = nxt;
+            e += 32;
+            nxt = e < e1 ? __ldg(ient + e) : kEllEmpty;
+            vload<T, VPL>(Xh + (size_t)(block_off + (ent & rmask)) * Rp, xv);
+#else
         for (uint32_t e = e0; e < e1; e += 32) {
             const uint32_t ent = __ldg(ient + e);
             if (ent == kEllEmpty) break;
             vload<T, VPL>(Xh + (size_t)(block_off + (ent & rmask)) * Rp, xv);
+#endif
             A cr, ci;
             if (UNIF) {
                 cr = u_ar;

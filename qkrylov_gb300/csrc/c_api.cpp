@@ -390,6 +390,15 @@ int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int*
     return QKRYLOV_SUCCESS;
 }
 
+int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, double* ms) {
+    if (!h || !h->ptr || !variant) return QKRYLOV_ERROR_INVALID_ARG;
+    const auto& H = *h->ptr;
+    *variant = H.fast() ? (int)H.variant(fp32 ? 8 : 16) : -1;
+    if (ms)
+        for (int v = 0; v < 3; ++v) ms[v] = H.tuned_ms(fp32 ? 0 : 1, v);
+    return QKRYLOV_SUCCESS;
+}
+
 int qkrylov_hamiltonian_benchmark_apply(qkrylov_hamiltonian_h h, int fp32, int reps, double* ms) {
     if (!h || !h->ptr || !ms || reps <= 0) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
@@ -690,16 +699,19 @@ qkg::BlockOpts block_opts(int n_vec, int n_steps, int mixed, int start_kind, uin
 extern "C" {
 
 int qkrylov_block_lanczos_tridiag(const qkrylov_hamiltonian_h* hams, int n_ham, int n_vec, int n_steps, int mixed,
-                                  int start_kind, uint64_t seed, const double* start_vectors, double* alphas,
+                                  int vectors_per_lane, int start_kind, uint64_t seed, const double* start_vectors,
+                                  double* alphas,
                                   double* betas, int* n_alpha, int* n_beta, double* norm2,
                                   qkrylov_block_stats_t* stats) {
     std::vector<qkg::Hamiltonian*> hs;
     if (!collect_hams(hams, n_ham, hs) || n_vec < 1 || n_vec > 32 || n_steps < 0 || !alphas || !betas || !n_alpha ||
-        !n_beta || !norm2 || (start_kind == QKRYLOV_START_GIVEN && !start_vectors))
+        !n_beta || !norm2 || (start_kind == QKRYLOV_START_GIVEN && !start_vectors) ||
+        (vectors_per_lane != 0 && vectors_per_lane != 1 && vectors_per_lane != 2 && vectors_per_lane != 4))
         return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         set_device(hams[0]);
         qkg::BlockOpts o = block_opts(n_vec, n_steps, mixed, start_kind, seed);
+        o.vpl = vectors_per_lane;
         if (o.start == qkg::BlockStart::Given) {
             const cd* p = reinterpret_cast<const cd*>(start_vectors);
             for (auto* H : hs)
@@ -745,7 +757,7 @@ int qkrylov_cf_block_f64(qkrylov_hamiltonian_h h, const double* phi0, int n_rhs,
         !norms)
         return QKRYLOV_ERROR_INVALID_ARG;
     std::vector<double> n2((size_t)n_rhs);
-    const int rc = qkrylov_block_lanczos_tridiag(&h, 1, n_rhs, n_iter, mixed, QKRYLOV_START_GIVEN, 0, phi0, alphas,
+    const int rc = qkrylov_block_lanczos_tridiag(&h, 1, n_rhs, n_iter, mixed, 0, QKRYLOV_START_GIVEN, 0, phi0, alphas,
                                                  betas, n_alpha, n_beta, n2.data(), stats);
     if (rc == QKRYLOV_SUCCESS)
         for (int i = 0; i < n_rhs; ++i) {

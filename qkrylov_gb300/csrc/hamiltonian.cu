@@ -419,8 +419,18 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
 constexpr int kRowsPerThread = 4;
 static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread rows per thread");
 
+// Resident CTAs per SM the register allocation is held to (FP32 / FP64).
+#ifndef QKG_ROWS_MINB
+#define QKG_ROWS_MINB 5
+#endif
+#ifndef QKG_ROWS_MINB64
+#define QKG_ROWS_MINB64 2
+#endif
+#ifndef QKG_ELL_PREFETCH
+#define QKG_ELL_PREFETCH 1
+#endif
 template <class T, class A, bool REAL, bool UNIF, bool OJ>
-__global__ void __launch_bounds__(kBlock) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
                                                            typename V2<T>::t* __restrict__ y_in) {
     using T2 = typename V2<T>::t;
     constexpr int RT = kRowsPerThread;
@@ -522,6 +532,42 @@ __global__ void __launch_bounds__(kBlock) spmv_rows_kernel(const FastParams<A> p
         }
     }
     // the four rows' ELL walks, slot by slot
+#if QKG_ELL_PREFETCH
+    // the next slot's entries are loaded while this slot's gathers are in flight
+    uint32_t cur[RT];
+#pragma unroll
+    for (int q = 0; q < RT; ++q) cur[q] = e0[q] < e1[q] ? __ldg(p.ient + e0[q]) : kEllEmpty;
+    bool more = true;
+    while (more) {
+        uint32_t nxt[RT];
+        T2 xv[RT];
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            e0[q] += 32;
+            nxt[q] = (cur[q] != kEllEmpty && e0[q] < e1[q]) ? __ldg(p.ient + e0[q]) : kEllEmpty;
+            if (cur[q] != kEllEmpty) xv[q] = x[block_off + (cur[q] & rmask)];
+        }
+        more = false;
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            if (cur[q] != kEllEmpty) {
+                if (UNIF) {
+                    cmac<A>(ar_[q], ai_[q], p.u_ar, p.u_ai, xv[q], REAL);
+                } else {
+                    const uint32_t t = cur[q] >> (p.rbits + 1);
+                    A cr = s_iamp[2 * t], ci = s_iamp[2 * t + 1];
+                    if ((cur[q] >> p.rbits) & 1u) {
+                        cr = -cr;
+                        ci = -ci;
+                    }
+                    cmac<A>(ar_[q], ai_[q], cr, ci, xv[q], REAL);
+                }
+            }
+            cur[q] = nxt[q];
+            more = more || (nxt[q] != kEllEmpty);
+        }
+    }
+#else
     bool more = true;
     while (more) {
         more = false;
@@ -556,6 +602,7 @@ __global__ void __launch_bounds__(kBlock) spmv_rows_kernel(const FastParams<A> p
             more = more || (e0[q] < e1[q]);
         }
     }
+#endif
     for (int k = 0; k < p.n_mixed; ++k) {
         const uint32_t C = mixed[k].C, V = mixed[k].V;
 #pragma unroll

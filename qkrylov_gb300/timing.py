@@ -1,7 +1,11 @@
-"""Time the SpMV kernel on a chain model (also the command the kernel
+"""Time the SpMV kernels on a chain model (also the commands the kernel
 profiles are taken with).
 
     python -m qkrylov_gb300.timing --model heisenberg --L 28 --precision fp32 --mode 0 --reps 5
+    python -m qkrylov_gb300.timing --L 22 --block 32 --steps 3 --vpl 4
+
+The second form runs the batched Lanczos on every Sz sector of the chain with
+``--block`` Philox start vectors per sector and reports the block-SpMV time.
 
 Builds the Hamiltonian (Heisenberg chain ``Sz Sz + 0.5 (S+ S- + S- S+)`` per
 bond, or Fermi-Hubbard chain ``-t c^dag c`` hopping per spin and direction plus
@@ -17,14 +21,14 @@ import time
 import qkrylov_gb300 as qk
 
 
-def heisenberg_chain(L, pbc=True, J=1.0):
+def heisenberg_chain(L, pbc=True, J=1.0, sz2=0):
     ops = qk.OpSum()
     for i in range(L if pbc else L - 1):
         j = (i + 1) % L
         ops.add_term(J, "Sz", i, "Sz", j)
         ops.add_term(0.5 * J, "Sp", i, "Sm", j)
         ops.add_term(0.5 * J, "Sm", i, "Sp", j)
-    return qk.SpinHalfBasis(L, conserve_sz=True, sz=0), qk.SpinHalfSite(), ops
+    return qk.SpinHalfBasis(L, conserve_sz=True, sz=sz2 / 2), qk.SpinHalfSite(), ops
 
 
 def hubbard_chain(L, pbc=True, t=1.0, U=4.0):
@@ -47,7 +51,12 @@ def main():
     p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     p.add_argument("--mode", type=int, default=0, help="0 autotuned, 1 generic, 2 fast, 3 fast staged, 4 fast rows4")
     p.add_argument("--reps", type=int, default=5)
+    p.add_argument("--block", type=int, default=0, help="vectors per sector: batched Lanczos over all Sz sectors")
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--vpl", type=int, default=0, help="block SpMV vectors per lane (0: autotuned)")
     a = p.parse_args()
+    if a.block:
+        return block(a)
     build = heisenberg_chain if a.model == "heisenberg" else hubbard_chain
     basis, site, ops = build(a.L, not a.obc)
     t0 = time.perf_counter()
@@ -61,6 +70,23 @@ def main():
     print(json.dumps({"model": a.model, "L": a.L, "pbc": not a.obc, "dim": n, "precision": a.precision,
                       "mode": a.mode, "fast": fast, "ms": ms, "alg_GBs": 2 * n * e / ms / 1e6,
                       "construct_s": round(tc, 3)}), flush=True)
+
+
+def block(a):
+    t0 = time.perf_counter()
+    hams = []
+    for sz2 in range(-a.L, a.L + 1, 2):
+        hams.append(qk.MatrixFreeHamiltonian(*heisenberg_chain(a.L, not a.obc, sz2=sz2)))
+    tc = time.perf_counter() - t0
+    mixed = a.precision == "fp32"
+    r = qk.block_lanczos_tridiag(hams, a.block, a.steps, mixed=mixed, start="philox", seed=1, vpl=a.vpl)
+    st = r.stats
+    e = 8 if mixed else 16
+    print(json.dumps({"model": "heisenberg", "L": a.L, "sectors": len(hams), "rows": st["rows"],
+                      "vectors_per_sector": a.block, "steps": a.steps, "precision": a.precision,
+                      "vectors_per_lane": st["vectors_per_lane"], "spmv_ms": st["spmv_ms"],
+                      "spmv_alg_GBs": 2 * st["rows"] * st["padded_vectors"] * e / st["spmv_ms"] / 1e6,
+                      "loop_s": st["seconds"], "tune_ms": st["tune_ms"], "construct_s": round(tc, 3)}), flush=True)
 
 
 if __name__ == "__main__":

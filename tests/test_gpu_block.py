@@ -154,3 +154,22 @@ def test_block_rejects_bad_arguments(qk):
         qk.block_lanczos_tridiag(hams, 33, 4)
     with pytest.raises(qk.QKrylovError):
         qk.ftlm_sectors(hams, [1.0], n_random=0)
+
+
+@pytest.mark.parametrize("R", [1, 2, 8, 32])
+def test_block_tile_shapes_agree(qk, R):
+    # every vectors-per-lane tile computes the same row sums; only the order of
+    # the per-CTA reduction partials differs
+    hams, _ = chain_sectors(qk, 12)
+    ref = None
+    for vpl in (1, 2, 4):
+        if R % vpl or R // vpl > 32:
+            continue
+        r = qk.block_lanczos_tridiag(hams, R, 10, mixed=False, start="philox", seed=2, vpl=vpl)
+        assert r.stats["vectors_per_lane"] == vpl
+        if ref is None:
+            ref = r
+            continue
+        for i in range(len(r.alphas)):
+            n = min(len(r.alphas[i]), len(ref.alphas[i]), 6)
+            assert np.abs(r.alphas[i][:n] - ref.alphas[i][:n]).max(initial=0) <= 1e-12 * 8
