@@ -48,6 +48,7 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ftlm", action="store_true", help="skip the batched FTLM measurement")
+    p.add_argument("--no-cf", action="store_true", help="skip the batched S(q, omega) measurement")
     p.add_argument("--cpu-sample-rows", type=int, default=1 << 19)
     return p.parse_args()
 
@@ -306,6 +307,8 @@ def main():
         out["dE0_vs_fp64"] = {"abs": de, "rel": de / abs(r64.energy), "meets_1e-10": de <= 1e-10 * abs(r64.energy)}
     if not args.no_ftlm:
         out["ftlm"] = ftlm_batch(qk, args.seed, hbm_peak, peak_kind)
+    if not args.no_cf:
+        out["cf"] = cf_batch(qk, hbm_peak, peak_kind)
     if ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_sample_rows, os.cpu_count() or 1)
     print(json.dumps(out), flush=True)
@@ -357,6 +360,56 @@ def ftlm_batch(qk, seed, hbm_peak, peak_kind):
             "mixed_vs_fp64": {"max_abs_dE": float(dE.max()) if dE.size else None,
                               "max_abs_dCv": float(dC.max()) if dC.size else None},
             "start_vectors": "seeded Philox Gaussian (device)"}
+
+
+CF_L, CF_STEPS, CF_NOMEGA, CF_ETA = 26, 300, 2000, 0.05
+
+
+def cf_batch(qk, hbm_peak, peak_kind):
+    """S(q, omega) of the Heisenberg chain L=26 periodic, Sz=0 (dim 10,400,600):
+    FP64 Lanczos ground state psi0, right-hand sides Sz(q)|psi0> with
+    Sz(q) = L^-1/2 sum_j e^{iqj} Sz_j for q = 2 pi k / 26, k = 0..13 (applied
+    as OpSum operators; k = 0 is the zero vector), then all 14 continued
+    fractions in one batched run of 300 steps (mixed form, and FP64 for the
+    comparison), S on 2000 omega in [0, 4] with eta = 0.05."""
+    import models as M
+    from conftest import make_model
+    b, s, o = make_model(qk, M.SPIN, CF_L, M.sector(sz2=0), M.heisenberg_terms(CF_L, True))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    t0 = time.perf_counter()
+    gs = qk.lanczos_ground_state(H, maxiter=300, tol=1e-12, mixed=False)
+    t_gs = time.perf_counter() - t0
+    psi, E0 = gs.eigenvector, gs.energy
+    t0 = time.perf_counter()
+    phis = []
+    for k in range(CF_L // 2 + 1):
+        ph = np.exp(2j * np.pi * k / CF_L * np.arange(CF_L)) / np.sqrt(CF_L)
+        ops = qk.OpSum()
+        for j in range(CF_L):
+            ops.add_term(ph[j], "Sz", j)
+        phis.append(qk.MatrixFreeHamiltonian(b, qk.SpinHalfSite(), ops).apply(psi))
+    t_rhs = time.perf_counter() - t0
+    omegas = np.linspace(0.0, 4.0, CF_NOMEGA)
+    out = {}
+    for mixed in (True, False):
+        t0 = time.perf_counter()
+        S, res, st = qk.spectral_functions_block(H, phis, omegas, E0, eta=CF_ETA, n_iter=CF_STEPS, mixed=mixed)
+        out[mixed] = (S, st, time.perf_counter() - t0)
+    S32, st32, w32 = out[True]
+    S64, st64, _ = out[False]
+    nrhs = len(phis)
+    alg = 2 * st32["rows"] * st32["padded_vectors"] * 8
+    achieved = alg / (st32["spmv_ms"] * 1e-3) / 1e9
+    return {"workload": f"heisenberg_chain_L{CF_L}_pbc_sz0_Szq_{nrhs}_rhs_{CF_STEPS}_steps_{CF_NOMEGA}_omega",
+            "dim": H.dimension, "rhs": nrhs, "E0": E0, "ground_state_s": t_gs, "rhs_build_s": t_rhs,
+            "rhs_steps_per_s": nrhs * CF_STEPS / st32["seconds"], "loop_s": st32["seconds"],
+            "e2e_s": w32, "fp64_rhs_steps_per_s": nrhs * CF_STEPS / st64["seconds"], "fp64_loop_s": st64["seconds"],
+            "tile": {"vectors_per_lane": st32["vectors_per_lane"], "padded_vectors": st32["padded_vectors"]},
+            "roofline": {"kernel": "spmv_block_kernel<float> (FP32 block SpMV, 16 vectors)", "bound": "hbm",
+                         "achieved": achieved, "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "algorithmic_bytes_per_launch": alg,
+                         "launch_ms": st32["spmv_ms"]},
+            "mixed_vs_fp64_max_rel_dS": float(np.abs(S32 - S64).max() / np.abs(S64).max())}
 
 
 def _cudart():

@@ -283,6 +283,10 @@ int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int*
  * not timed). */
 int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, double* ms_per_variant);
 
+/* States first .. first + count - 1 of a basis in the reference's order and
+ * bit encoding (qkrylov_basis_state for a range). */
+int qkrylov_basis_states(qkrylov_basis_h basis, uint64_t first, uint64_t count, uint64_t* out);
+
 /* Time `reps` back-to-back applies of the FP32 (fp32 != 0) or FP64 kernel on
  * internal device vectors, with CUDA events on the Hamiltonian's stream;
  * *ms_per_apply receives the mean launch duration. */

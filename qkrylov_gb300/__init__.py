@@ -128,6 +128,7 @@ _SIGS = {
     "qkrylov_hamiltonian_entries": (_i, [_vp, _u64p, _u64p, _u64p, _dp]),
     "qkrylov_hamiltonian_select_kernel": (_i, [_vp, _i, _ip]),
     "qkrylov_hamiltonian_tuning": (_i, [_vp, _i, _ip, _dp]),
+    "qkrylov_basis_states": (_i, [_vp, _u64, _u64, _u64p]),
     "qkrylov_hamiltonian_benchmark_apply": (_i, [_vp, _i, _i, _dp]),
 }
 
@@ -234,8 +235,12 @@ class Basis(_Handle):
     def contains(self, s):
         return bool(lib().qkrylov_basis_contains(self._h, int(s)))
 
-    def states(self):
-        return _np.array([self.state(i) for i in range(self.size)], dtype=_np.uint64)
+    def states(self, first=0, count=None):
+        """States (reference order and bit encoding) as a uint64 array."""
+        n = self.size - first if count is None else int(count)
+        out = _np.zeros(max(0, n), dtype=_np.uint64)
+        _check(lib().qkrylov_basis_states(self._h, int(first), out.size, out.ctypes.data_as(_u64p)))
+        return out
 
 
 class SpinHalfBasis(Basis):
@@ -589,6 +594,19 @@ def block_lanczos_tridiag(hams, n_vec, n_steps, mixed=True, start="ftlm", seed=0
     b = b.reshape(nv, -1)
     return BlockTridiagResult([a[i, : na[i]].copy() for i in range(nv)], [b[i, : nb[i]].copy() for i in range(nv)],
                               n2, _stats(st))
+
+
+def spectral_functions_block(H, phis, omegas, E0, eta=0.05, n_iter=100, mixed=True):
+    """S_r(omega) (evaluate_spectral_function, dynamics.cpp:61-89) for several
+    right-hand sides from one batched continued-fraction run; rows of zeros
+    for zero right-hand sides.  Returns (S[r, omega], [DynamicsResult], stats)."""
+    res, st = continued_fraction_block(H, phis, n_iter=n_iter, mixed=mixed)
+    om = _np.atleast_1d(_np.asarray(omegas, dtype=_np.float64))
+    S = _np.zeros((len(res), om.size))
+    for i, r in enumerate(res):
+        if len(r.alphas):
+            S[i] = evaluate_spectral_function(r, om, E0, eta)
+    return S, res, st
 
 
 class FTLMSectorsResult:

@@ -196,6 +196,15 @@ uint64_t qkrylov_basis_state(qkrylov_basis_h b, uint64_t i) {
     if (!b || !b->ptr) return 0;
     try { return b->ptr->state_ref(i); } catch (const std::exception& e) { fail(e); return 0; }
 }
+int qkrylov_basis_states(qkrylov_basis_h b, uint64_t first, uint64_t count, uint64_t* out) {
+    if (!b || !b->ptr || (count && !out)) return QKRYLOV_ERROR_INVALID_ARG;
+    if (first > b->ptr->dim || count > b->ptr->dim - first) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        const qkg::Basis& B = *b->ptr;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)count; ++i) out[i] = B.state_ref(first + (uint64_t)i);
+    });
+}
 int64_t qkrylov_basis_index(qkrylov_basis_h b, uint64_t s) {
     if (!b || !b->ptr) return -1;
     try { return b->ptr->index_ref(s); } catch (const std::exception& e) { fail(e); return -1; }

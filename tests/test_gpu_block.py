@@ -173,3 +173,38 @@ def test_block_tile_shapes_agree(qk, R):
         for i in range(len(r.alphas)):
             n = min(len(r.alphas[i]), len(ref.alphas[i]), 6)
             assert np.abs(r.alphas[i][:n] - ref.alphas[i][:n]).max(initial=0) <= 1e-12 * 8
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_structure_factor_block(qk, oracle, mixed):
+    # S(q, omega) right-hand sides Sz(q)|psi0> built by applying an OpSum
+    # operator to the ground state; all q in one batched run
+    L = 10
+    m = (M.SPIN, L, M.sector(sz2=0), M.heisenberg_terms(L, True))
+    b, s, o = make_model(qk, *m)
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    gs = qk.lanczos_ground_state(H, maxiter=200, tol=1e-12)
+    psi, E0 = gs.eigenvector, gs.energy
+    st = b.states()
+    assert st.size == H.dimension and np.array_equal(st[:3], [b.state(i) for i in range(3)])
+    sz = ((st[:, None] >> np.arange(L, dtype=np.uint64)) & np.uint64(1)).astype(float) - 0.5
+    phis = []
+    for k in range(L // 2 + 1):
+        ph = np.exp(2j * np.pi * k / L * np.arange(L)) / np.sqrt(L)
+        ops = qk.OpSum()
+        for j in range(L):
+            ops.add_term(ph[j], "Sz", j)
+        phi = qk.MatrixFreeHamiltonian(b, qk.SpinHalfSite(), ops).apply(psi)
+        # the matrix elements are the conjugated term amplitudes
+        # (matrix_free_hamiltonian.cpp stores conj(amp)), so this applies Sz(-q)
+        np.testing.assert_allclose(phi, psi * (sz @ np.conj(ph)), atol=1e-13)
+        phis.append(phi)
+    omegas = np.linspace(0.0, 4.0, 81)
+    S, res, stats = qk.spectral_functions_block(H, phis, omegas, E0, eta=0.05, n_iter=60, mixed=mixed)
+    assert np.all(S[0] == 0.0) and res[0].norm_phi0 == 0.0  # q = 0: total Sz = 0 in this sector
+    oh = OHam(oracle, *m)
+    for k in range(1, len(phis)):
+        a, bb, nrm = oh.cf(phis[k], 60)
+        So = np.array([spectral(oracle, a, bb, nrm, w, E0, 0.05) for w in omegas])
+        tol = OBS_RTOL if not mixed else MIXED_RTOL
+        assert np.abs(S[k] - So).max() <= tol * np.abs(So).max()
