@@ -577,6 +577,26 @@ int qkrylov_davidson_lowest_complex_f64(qkrylov_hamiltonian_h h, int n_eig, int 
     });
 }
 
+int qkrylov_davidson_lowest_ex(qkrylov_hamiltonian_h h, int n_eig, int max_sub, double tol, int mixed, double* evals,
+                               double* evecs, double* residuals, qkrylov_davidson_result_c_t* info, double* seconds) {
+    if (!h || !h->ptr || !evals || n_eig <= 0) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        set_device(h);
+        const auto res = mixed ? qkg::davidson_mixed(*h->ptr, n_eig, max_sub, tol, evecs != nullptr)
+                               : qkg::davidson_f64(*h->ptr, n_eig, max_sub, tol, evecs != nullptr);
+        const size_t k = std::min<size_t>((size_t)n_eig, res.evals.size());
+        for (size_t i = 0; i < k; ++i) evals[i] = res.evals[i];
+        if (residuals)
+            for (size_t i = 0; i < k; ++i) residuals[i] = i < res.residuals.size() ? res.residuals[i] : -1.0;
+        if (info) { info->iterations = res.iters; info->converged = res.converged ? 1 : 0; }
+        if (seconds) *seconds = res.seconds;
+        if (evecs) {
+            const uint64_t n = h->ptr->dim();
+            for (size_t j = 0; j < k && j < res.evecs.size(); ++j) std::memcpy(evecs + j * 2 * n, res.evecs[j].data(), n * sizeof(cd));
+        }
+    });
+}
+
 int qkrylov_continued_fraction_coeffs_complex(qkrylov_hamiltonian_h h, const float* phi0, int n_iter, float* alphas,
                                               float* betas, float* norm, int* num) {
     if (!h || !h->ptr || !phi0 || !alphas || !betas || !norm || n_iter <= 0) return QKRYLOV_ERROR_INVALID_ARG;

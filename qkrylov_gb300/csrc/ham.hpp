@@ -203,7 +203,15 @@ void mcombine_f64(const double2* const* V_dev, int k, const std::complex<double>
                   Workspace& ws, cudaStream_t s);
 void mcombine_f32(const float2* const* V_dev, int k, const std::complex<double>* c, float2* w, uint64_t n,
                   Workspace& ws, cudaStream_t s);
+// W_o = (accumulate ? W_o : 0) + sum_j c[o * k + j] V_j for o < nout <= 8 (one
+// pass over the V_j; V and W given as device pointer arrays for V, host array
+// of device pointers for W; c on the host, nout * k <= 1024).
+void mcombine_multi_f64(const double2* const* V_dev, int k, const std::complex<double>* c, double2* const* W, int nout,
+                        uint64_t n, bool accumulate, Workspace& ws, cudaStream_t s);
+void mcombine_multi_f32(const float2* const* V_dev, int k, const std::complex<double>* c, float2* const* W, int nout,
+                        uint64_t n, bool accumulate, Workspace& ws, cudaStream_t s);
 // Davidson preconditioner t_i = r_i / (d_i - lambda) with the reference's clamp.
 void davidson_precond_f64(const double2* r, const double2* d, double lambda, double2* t, uint64_t n, cudaStream_t s);
+void davidson_precond_f32(const float2* r, const double2* d, double lambda, float2* t, uint64_t n, cudaStream_t s);
 
 }  // namespace qkg

@@ -256,21 +256,82 @@ __global__ void mdot_kernel(const T2* const* __restrict__ V, int k, const T2* __
 template <class T2, class A>
 __global__ void mcomb_kernel(const T2* const* __restrict__ V, int k, const double2* __restrict__ c, T2* __restrict__ w,
                              uint64_t n) {
-    extern __shared__ double2 sc[];
-    for (int j = threadIdx.x; j < k; j += blockDim.x) sc[j] = c[j];
+    // coefficients converted to the working type once (a double-to-float
+    // conversion per element would run on the FP64 pipe)
+    extern __shared__ double2 sc_raw[];
+    A* sc = reinterpret_cast<A*>(sc_raw);
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+        sc[2 * j] = (A)c[j].x;
+        sc[2 * j + 1] = (A)c[j].y;
+    }
     __syncthreads();
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         T2 o = w[i];
         A re = (A)o.x, im = (A)o.y;
         for (int j = 0; j < k; ++j) {
             const T2 a = V[j][i];
-            const A cr = (A)sc[j].x, ci = (A)sc[j].y;
+            const A cr = sc[2 * j], ci = sc[2 * j + 1];
             re = fma(cr, (A)a.x, fma(-ci, (A)a.y, re));
             im = fma(cr, (A)a.y, fma(ci, (A)a.x, im));
         }
         o.x = re;
         o.y = im;
         w[i] = o;
+    }
+}
+
+// W_o = (accumulate ? W_o : 0) + sum_j C[o * k + j] V_j for o < nout: each
+// V_j is read once for all outputs.
+template <class T2, class A, int NOUT>
+__global__ void mcomb_multi_kernel(const T2* const* __restrict__ V, int k, const double2* __restrict__ c,
+                                   T2* const* __restrict__ W, uint64_t n, int accumulate) {
+    extern __shared__ double2 sc_raw[];
+    A* sc = reinterpret_cast<A*>(sc_raw);
+    for (int j = threadIdx.x; j < NOUT * k; j += blockDim.x) {
+        sc[2 * j] = (A)c[j].x;
+        sc[2 * j + 1] = (A)c[j].y;
+    }
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        A re[NOUT], im[NOUT];
+#pragma unroll
+        for (int o = 0; o < NOUT; ++o) {
+            re[o] = 0;
+            im[o] = 0;
+            if (accumulate) {
+                const T2 w = W[o][i];
+                re[o] = (A)w.x;
+                im[o] = (A)w.y;
+            }
+        }
+        for (int j = 0; j < k; ++j) {
+            const T2 a = V[j][i];
+#pragma unroll
+            for (int o = 0; o < NOUT; ++o) {
+                const A cr = sc[2 * (o * k + j)], ci = sc[2 * (o * k + j) + 1];
+                re[o] = fma(cr, (A)a.x, fma(-ci, (A)a.y, re[o]));
+                im[o] = fma(cr, (A)a.y, fma(ci, (A)a.x, im[o]));
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < NOUT; ++o) {
+            T2 w;
+            w.x = re[o];
+            w.y = im[o];
+            W[o][i] = w;
+        }
+    }
+}
+
+// The Davidson preconditioner for FP32 vectors (difference taken in FP64).
+__global__ void precond32_kernel(const float2* __restrict__ r, const double2* __restrict__ d, double lambda,
+                                 float2* __restrict__ t, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float fr = (float)(d[i].x - lambda), fi = (float)d[i].y;
+        if (sqrtf(fr * fr + fi * fi) < 1e-10f) { fr = (fr >= 0.f) ? 1e-10f : -1e-10f; fi = 0.f; }
+        const float2 a = r[i];
+        const float den = fr * fr + fi * fi;
+        t[i] = make_float2((a.x * fr + a.y * fi) / den, (a.y * fr - a.x * fi) / den);
     }
 }
 
@@ -428,6 +489,46 @@ void philox_normal_f64(uint64_t seed, uint64_t stream, double2* out, uint64_t n,
 }
 void philox_normal_f32(uint64_t seed, uint64_t stream, float2* out, uint64_t n, cudaStream_t s) {
     philox_normal_kernel<float2, false><<<stream_grid(n), kThreads, 0, s>>>(seed, stream, out, n);
+    QKG_LAUNCHED();
+}
+template <class T2, class A>
+static void mcomb_multi_impl(const T2* const* V, int k, const std::complex<double>* c, T2* const* W, int nout,
+                             uint64_t n, bool accumulate, Workspace& ws, cudaStream_t s) {
+    QKG_REQUIRE(nout >= 1 && nout <= 8, "mcombine_multi: 1..8 outputs");
+    QKG_REQUIRE(k >= 0 && nout * k <= 1024, "mcombine_multi: at most 1024 coefficients");
+    if (!n) return;
+    // coefficients and the output pointer table go through the workspace result slots
+    double2* dc = ws.result.as<double2>();
+    QKG_CUDA(cudaMemcpyAsync(dc, c, (size_t)nout * k * sizeof(double2), cudaMemcpyHostToDevice, s));
+    T2** dw = reinterpret_cast<T2**>(dc + 1024);
+    QKG_CUDA(cudaMemcpyAsync(dw, W, (size_t)nout * sizeof(T2*), cudaMemcpyHostToDevice, s));
+    const size_t sm = (size_t)nout * k * sizeof(double2);
+    const int g = stream_grid(n);
+    const int acc = accumulate ? 1 : 0;
+    switch (nout) {
+        case 1: mcomb_multi_kernel<T2, A, 1><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        case 2: mcomb_multi_kernel<T2, A, 2><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        case 3: mcomb_multi_kernel<T2, A, 3><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        case 4: mcomb_multi_kernel<T2, A, 4><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        case 5: mcomb_multi_kernel<T2, A, 5><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        case 6: mcomb_multi_kernel<T2, A, 6><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        case 7: mcomb_multi_kernel<T2, A, 7><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+        default: mcomb_multi_kernel<T2, A, 8><<<g, kThreads, sm, s>>>(V, k, dc, dw, n, acc); break;
+    }
+    QKG_LAUNCHED();
+    // the host arrays may be reused once the copies have been consumed
+    QKG_CUDA(cudaStreamSynchronize(s));
+}
+void mcombine_multi_f64(const double2* const* V, int k, const std::complex<double>* c, double2* const* W, int nout,
+                        uint64_t n, bool accumulate, Workspace& ws, cudaStream_t s) {
+    mcomb_multi_impl<double2, double>(V, k, c, W, nout, n, accumulate, ws, s);
+}
+void mcombine_multi_f32(const float2* const* V, int k, const std::complex<double>* c, float2* const* W, int nout,
+                        uint64_t n, bool accumulate, Workspace& ws, cudaStream_t s) {
+    mcomb_multi_impl<float2, float>(V, k, c, W, nout, n, accumulate, ws, s);
+}
+void davidson_precond_f32(const float2* r, const double2* d, double lambda, float2* t, uint64_t n, cudaStream_t s) {
+    precond32_kernel<<<stream_grid(n), kThreads, 0, s>>>(r, d, lambda, t, n);
     QKG_LAUNCHED();
 }
 void davidson_precond_f64(const double2* r, const double2* d, double lambda, double2* t, uint64_t n, cudaStream_t s) {

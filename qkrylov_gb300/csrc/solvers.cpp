@@ -8,6 +8,7 @@
 #include <limits>
 #include <numeric>
 #include <random>
+#include <type_traits>
 
 namespace qkg {
 
@@ -585,15 +586,73 @@ void ftlm_observables(const std::vector<FTLMTri>& tri, const double* betas, int 
 }
 
 // ============================================================ Davidson
-DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream) {
+namespace {
+// Vector operations of one storage precision.
+template <class T2> struct DavOps;
+template <> struct DavOps<double2> {
+    static void apply(Hamiltonian& H, const double2* x, double2* y, cudaStream_t s) { H.apply_f64(x, y, s); }
+    static void mdot(const double2* const* V, int k, const double2* w, uint64_t n, cd* o, Workspace& ws, cudaStream_t s) {
+        mdot_f64(V, k, w, n, o, ws, s);
+    }
+    static void mcomb(const double2* const* V, int k, const cd* c, double2* w, uint64_t n, Workspace& ws, cudaStream_t s) {
+        mcombine_f64(V, k, c, w, n, ws, s);
+    }
+    static void mmulti(const double2* const* V, int k, const cd* c, double2* const* W, int no, uint64_t n, bool acc,
+                       Workspace& ws, cudaStream_t s) {
+        mcombine_multi_f64(V, k, c, W, no, n, acc, ws, s);
+    }
+    static double nrm2sq(const double2* x, uint64_t n, Workspace& ws, cudaStream_t s) { return nrm2sq_f64(x, n, ws, s); }
+    static void scal(double a, double2* x, uint64_t n, cudaStream_t s) { scal_f64(a, x, n, s); }
+    static void precond(const double2* r, const double2* d, double l, double2* t, uint64_t n, cudaStream_t s) {
+        davidson_precond_f64(r, d, l, t, n, s);
+    }
+    static void from64(const double2* x, double2* y, uint64_t n, cudaStream_t s) {
+        QKG_CUDA(cudaMemcpyAsync(y, x, n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    }
+    static void to64(const double2* x, double2* y, uint64_t n, cudaStream_t s) { from64(x, y, n, s); }
+};
+template <> struct DavOps<float2> {
+    static void apply(Hamiltonian& H, const float2* x, float2* y, cudaStream_t s) { H.apply_f32(x, y, s); }
+    static void mdot(const float2* const* V, int k, const float2* w, uint64_t n, cd* o, Workspace& ws, cudaStream_t s) {
+        mdot_f32(V, k, w, n, o, ws, s);
+    }
+    static void mcomb(const float2* const* V, int k, const cd* c, float2* w, uint64_t n, Workspace& ws, cudaStream_t s) {
+        mcombine_f32(V, k, c, w, n, ws, s);
+    }
+    static void mmulti(const float2* const* V, int k, const cd* c, float2* const* W, int no, uint64_t n, bool acc,
+                       Workspace& ws, cudaStream_t s) {
+        mcombine_multi_f32(V, k, c, W, no, n, acc, ws, s);
+    }
+    static double nrm2sq(const float2* x, uint64_t n, Workspace& ws, cudaStream_t s) { return nrm2sq_f32(x, n, ws, s); }
+    static void scal(double a, float2* x, uint64_t n, cudaStream_t s) { scal_f32(a, x, n, s); }
+    static void precond(const float2* r, const double2* d, double l, float2* t, uint64_t n, cudaStream_t s) {
+        davidson_precond_f32(r, d, l, t, n, s);
+    }
+    static void from64(const double2* x, float2* y, uint64_t n, cudaStream_t s) { f64_to_f32(x, y, n, s); }
+    static void to64(const float2* x, double2* y, uint64_t n, cudaStream_t s) { f32_to_f64(x, y, n, s); }
+};
+
+// src/solvers/davidson.cpp:86-227 with the Krylov vectors stored in T2.
+// Projections <V_i, HV_j> of vectors that did not change are kept from the
+// previous iteration (the reference recomputes them; the values are the same
+// dot products), the k residuals and the restart's Ritz vectors are formed in
+// one pass over V and HV each.  MIXED (FP32 storage): SpMV in FP32, projections
+// and norms by compensated reductions in FP64, corrections orthogonalised twice,
+// and the final Ritz pairs refined in FP64 (Rayleigh quotient, residual).
+template <class T2>
+DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream) {
+    using Op = DavOps<T2>;
+    constexpr bool MIXED = std::is_same<T2, float2>::value;
     DavidsonOut out;
     const uint64_t n = H.dim();
     if (n == 0) return out;
     cudaStream_t st = H.stream();
+    const auto t_start = std::chrono::steady_clock::now();
     n_eig = (int)std::min<uint64_t>((uint64_t)n_eig, n);
     max_sub = std::max(max_sub, 2 * n_eig);
+    QKG_REQUIRE(max_sub + n_eig <= 1024, "Davidson: subspace limited to 1024 vectors");
     Workspace ws(ws_cap(max_sub + n_eig + 2));
-    DBuf diag(n * sizeof(double2)), tmp;
+    DBuf diag(n * sizeof(double2)), tmp, d64(n * sizeof(double2));
     H.diagonal_f64(diag.as<double2>(), st);
     // Seeds: unit vectors at the n_eig smallest diagonal entries, in the order
     // std::sort leaves them (davidson.cpp:111-121); the diagonal is taken in the
@@ -610,110 +669,178 @@ DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, boo
             return dref[i].real() < dref[j].real() || (dref[i].real() == dref[j].real() && i < j);
         });
     }
+    std::vector<cd>().swap(dref);
     std::mt19937 rng(1234);
     std::uniform_real_distribution<double> dist(-1.0, 1.0);
     std::uniform_real_distribution<float> dist32(-1.0f, 1.0f);
-    VecList<double2> V(n), HV(n);
+    VecList<T2> V(n), HV(n);
     std::vector<cd> hv(n), c;
-    auto orthonormalize = [&](double2* t) -> double {
-        if (V.size()) {
+    const int passes = MIXED ? 2 : 1;
+    auto orthonormalize = [&](T2* t) -> double {
+        for (int p = 0; p < passes && V.size(); ++p) {
             c.assign(V.size(), 0.0);
-            mdot_f64(V.dev(), (int)V.size(), t, n, c.data(), ws, st);
+            Op::mdot(V.dev(), (int)V.size(), t, n, c.data(), ws, st);
             for (auto& x : c) x = -x;
-            mcombine_f64(V.dev(), (int)V.size(), c.data(), t, n, ws, st);
+            Op::mcomb(V.dev(), (int)V.size(), c.data(), t, n, ws, st);
         }
-        return std::sqrt(nrm2sq_f64(t, n, ws, st));
+        return std::sqrt(Op::nrm2sq(t, n, ws, st));
     };
-    DBuf seed(n * sizeof(double2));
+    DBuf seed(n * sizeof(T2));
     for (int i = 0; i < n_eig; ++i) {
         std::fill(hv.begin(), hv.end(), cd(0.0));
         hv[di[i]] = 1.0;
-        upload_ref_f64(H, hv.data(), seed.as<double2>(), tmp);
-        double nrm = orthonormalize(seed.as<double2>());
+        upload_ref_f64(H, hv.data(), d64.as<double2>(), tmp);
+        Op::from64(d64.as<double2>(), seed.as<T2>(), n, st);
+        double nrm = orthonormalize(seed.as<T2>());
         if (nrm < 1e-10) {
             if (f32_stream) fill_stream(rng, dist32, n, hv.data());
             else fill_stream(rng, dist, n, hv.data());
-            upload_ref_f64(H, hv.data(), seed.as<double2>(), tmp);
-            nrm = orthonormalize(seed.as<double2>());
+            upload_ref_f64(H, hv.data(), d64.as<double2>(), tmp);
+            Op::from64(d64.as<double2>(), seed.as<T2>(), n, st);
+            nrm = orthonormalize(seed.as<T2>());
         }
-        double2* v = V.push();
-        QKG_CUDA(cudaMemcpyAsync(v, seed.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-        scal_f64(1.0 / nrm, v, n, st);
-        H.apply_f64(v, HV.push(), st);
+        T2* v = V.push();
+        QKG_CUDA(cudaMemcpyAsync(v, seed.p, n * sizeof(T2), cudaMemcpyDeviceToDevice, st));
+        Op::scal(1.0 / nrm, v, n, st);
+        Op::apply(H, v, HV.push(), st);
     }
-    DBuf r(n * sizeof(double2));
+    std::vector<cd>().swap(hv);
+    // cached projected matrix: rows[i][j] = <V_i, HV_j> for j <= i < m_cached
+    std::vector<std::vector<cd>> rows;
+    std::vector<DBuf> rbuf(n_eig);
+    for (auto& r : rbuf) r.alloc(n * sizeof(T2));
+    std::vector<T2*> rptr;
+    for (auto& r : rbuf) rptr.push_back(r.as<T2>());
     for (int iter = 0; iter < 100; ++iter) {
         const int m = (int)V.size();
-        std::vector<cd> Hs((size_t)m * m);
-        std::vector<cd> col(m);
-        for (int j = 0; j < m; ++j) {
-            mdot_f64(V.dev(), m, HV[j], n, col.data(), ws, st);  // <V_i, HV_j>
-            for (int i = j; i < m; ++i) {
-                Hs[(size_t)i * m + j] = col[i];
-                if (i != j) Hs[(size_t)j * m + i] = std::conj(col[i]);
-            }
+        for (int i = (int)rows.size(); i < m; ++i) {
+            std::vector<cd> col(i + 1);
+            Op::mdot(HV.dev(), i + 1, V[i], n, col.data(), ws, st);  // <HV_j, V_i>
+            for (auto& x : col) x = std::conj(x);
+            rows.push_back(std::move(col));
         }
+        std::vector<cd> Hs((size_t)m * m);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j <= i; ++j) {
+                Hs[(size_t)i * m + j] = rows[i][j];
+                if (i != j) Hs[(size_t)j * m + i] = std::conj(rows[i][j]);
+            }
         std::vector<double> ev;
         std::vector<std::vector<cd>> evec;
         hermitian_eig(Hs, m, ev, evec);
+        // residuals r_k = HV s_k - lambda_k V s_k for all k (one pass over HV, one over V)
+        const int kc = std::max(1, std::min(8, 1024 / std::max(m, 1)));  // outputs per pass
+        for (int k0 = 0; k0 < n_eig; k0 += kc) {
+            const int nk = std::min(kc, n_eig - k0);
+            std::vector<cd> cs((size_t)nk * m), cl((size_t)nk * m);
+            for (int k = 0; k < nk; ++k)
+                for (int i = 0; i < m; ++i) {
+                    cs[(size_t)k * m + i] = evec[k0 + k][i];
+                    cl[(size_t)k * m + i] = -ev[k0 + k] * evec[k0 + k][i];
+                }
+            Op::mmulti(HV.dev(), m, cs.data(), rptr.data() + k0, nk, n, false, ws, st);
+            Op::mmulti(V.dev(), m, cl.data(), rptr.data() + k0, nk, n, true, ws, st);
+        }
         bool all_conv = true;
         std::vector<DBuf> corr;
+        out.residuals.assign(n_eig, 0.0);
         for (int k = 0; k < n_eig; ++k) {
-            const double lambda = ev[k];
-            QKG_CUDA(cudaMemsetAsync(r.p, 0, n * sizeof(double2), st));
-            std::vector<cd> cs(evec[k]), cl(m);
-            for (int i = 0; i < m; ++i) cl[i] = -lambda * evec[k][i];
-            mcombine_f64(HV.dev(), m, cs.data(), r.as<double2>(), n, ws, st);
-            mcombine_f64(V.dev(), m, cl.data(), r.as<double2>(), n, ws, st);
-            const double rn = std::sqrt(nrm2sq_f64(r.as<double2>(), n, ws, st));
+            const double rn = std::sqrt(Op::nrm2sq(rptr[k], n, ws, st));
+            out.residuals[k] = rn;
             if (rn > tol) {
                 all_conv = false;
-                DBuf t(n * sizeof(double2));
-                davidson_precond_f64(r.as<double2>(), diag.as<double2>(), lambda, t.as<double2>(), n, st);
+                DBuf t(n * sizeof(T2));
+                Op::precond(rptr[k], diag.as<double2>(), ev[k], t.as<T2>(), n, st);
                 corr.push_back(std::move(t));
             }
         }
         if (all_conv || iter == 99) {
             out.iters = iter + 1;
             out.converged = all_conv;
-            DBuf e(n * sizeof(double2));
-            for (int k = 0; k < n_eig; ++k) {
-                out.evals.push_back(ev[k]);
-                if (want_vecs) {
-                    QKG_CUDA(cudaMemsetAsync(e.p, 0, n * sizeof(double2), st));
-                    mcombine_f64(V.dev(), m, evec[k].data(), e.as<double2>(), n, ws, st);
+            out.evals.assign(ev.begin(), ev.begin() + n_eig);
+            // Ritz vectors (into the residual buffers)
+            std::vector<cd> cs((size_t)n_eig * m);
+            for (int k = 0; k < n_eig; ++k)
+                for (int i = 0; i < m; ++i) cs[(size_t)k * m + i] = evec[k][i];
+            for (int k0 = 0; k0 < n_eig; k0 += kc)
+                Op::mmulti(V.dev(), m, cs.data() + (size_t)k0 * m, rptr.data() + k0, std::min(kc, n_eig - k0), n, false,
+                           ws, st);
+            DBuf e64, h64;
+            if (MIXED) {
+                // FP64 refinement: Rayleigh quotient and residual of each normalised Ritz vector
+                V.clear();
+                HV.clear();
+                e64.alloc(n * sizeof(double2));
+                h64.alloc(n * sizeof(double2));
+                bool conv64 = true;
+                for (int k = 0; k < n_eig; ++k) {
+                    Op::to64(rptr[k], e64.as<double2>(), n, st);
+                    const double nr = std::sqrt(nrm2sq_f64(e64.as<double2>(), n, ws, st));
+                    if (nr > 0.0) scal_f64(1.0 / nr, e64.as<double2>(), n, st);
+                    H.apply_f64(e64.as<double2>(), h64.as<double2>(), st);
+                    const double lam = dot_f64(e64.as<double2>(), h64.as<double2>(), n, ws, st).real();
+                    axpy_f64(cd(-lam, 0.0), e64.as<double2>(), h64.as<double2>(), n, st);
+                    out.residuals[k] = std::sqrt(nrm2sq_f64(h64.as<double2>(), n, ws, st));
+                    out.evals[k] = lam;
+                    if (out.residuals[k] > tol) conv64 = false;
+                    if (want_vecs) {
+                        std::vector<cd> h(n);
+                        download_ref_f64(H, e64.as<double2>(), h.data(), tmp);
+                        out.evecs.push_back(std::move(h));
+                    }
+                }
+                out.converged = conv64;
+            } else if (want_vecs) {
+                for (int k = 0; k < n_eig; ++k) {
                     std::vector<cd> h(n);
-                    download_ref_f64(H, e.as<double2>(), h.data(), tmp);
+                    download_ref_f64(H, reinterpret_cast<const double2*>(rptr[k]), h.data(), tmp);
                     out.evecs.push_back(std::move(h));
                 }
             }
             QKG_CUDA(cudaStreamSynchronize(st));
+            out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
             return out;
         }
         if (V.size() + corr.size() > (size_t)max_sub) {  // restart to the Ritz vectors (:196-211)
             std::vector<DBuf> nv, nh;
+            std::vector<T2*> pv, ph;
             for (int k = 0; k < n_eig; ++k) {
-                nv.emplace_back(n * sizeof(double2));
-                nh.emplace_back(n * sizeof(double2));
-                QKG_CUDA(cudaMemsetAsync(nv.back().p, 0, n * sizeof(double2), st));
-                QKG_CUDA(cudaMemsetAsync(nh.back().p, 0, n * sizeof(double2), st));
-                mcombine_f64(V.dev(), m, evec[k].data(), nv.back().as<double2>(), n, ws, st);
-                mcombine_f64(HV.dev(), m, evec[k].data(), nh.back().as<double2>(), n, ws, st);
+                nv.emplace_back(n * sizeof(T2));
+                nh.emplace_back(n * sizeof(T2));
+                pv.push_back(nv.back().as<T2>());
+                ph.push_back(nh.back().as<T2>());
+            }
+            std::vector<cd> cs((size_t)n_eig * m);
+            for (int k = 0; k < n_eig; ++k)
+                for (int i = 0; i < m; ++i) cs[(size_t)k * m + i] = evec[k][i];
+            for (int k0 = 0; k0 < n_eig; k0 += kc) {
+                const int nk = std::min(kc, n_eig - k0);
+                Op::mmulti(V.dev(), m, cs.data() + (size_t)k0 * m, pv.data() + k0, nk, n, false, ws, st);
+                Op::mmulti(HV.dev(), m, cs.data() + (size_t)k0 * m, ph.data() + k0, nk, n, false, ws, st);
             }
             V.take(nv);
             HV.take(nh);
+            rows.clear();
         }
         for (auto& t : corr) {  // orthogonalise each correction and extend (:213-223)
-            const double nrm = orthonormalize(t.as<double2>());
+            const double nrm = orthonormalize(t.as<T2>());
             if (nrm > 1e-10) {
-                scal_f64(1.0 / nrm, t.as<double2>(), n, st);
-                double2* v = V.push();
-                QKG_CUDA(cudaMemcpyAsync(v, t.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-                H.apply_f64(v, HV.push(), st);
+                Op::scal(1.0 / nrm, t.as<T2>(), n, st);
+                T2* v = V.push();
+                QKG_CUDA(cudaMemcpyAsync(v, t.p, n * sizeof(T2), cudaMemcpyDeviceToDevice, st));
+                Op::apply(H, v, HV.push(), st);
             }
         }
     }
     return out;
+}
+}  // namespace
+
+DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream) {
+    return davidson_impl<double2>(H, n_eig, max_sub, tol, want_vecs, f32_stream);
+}
+DavidsonOut davidson_mixed(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs) {
+    return davidson_impl<float2>(H, n_eig, max_sub, tol, want_vecs, false);
 }
 
 }  // namespace qkg

@@ -124,7 +124,17 @@ void ftlm_observables(const std::vector<FTLMTri>& tri, const double* betas, int 
                       bool shifted, double* log_zmax);
 
 // ---- Davidson (src/solvers/davidson.cpp:86-227) -------------------------------
-struct DavidsonOut { std::vector<double> evals; std::vector<std::vector<cd>> evecs; int iters = 0; bool converged = false; };
+struct DavidsonOut {
+    std::vector<double> evals;
+    std::vector<std::vector<cd>> evecs;
+    int iters = 0;
+    bool converged = false;
+    std::vector<double> residuals;  // ||H v - lambda v|| of the returned pairs (FP64 for the mixed form)
+    double seconds = 0.0;
+};
 DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream = false);
+// Mixed form: FP32 Krylov vectors and SpMV, FP64-accurate (compensated) projections
+// and norms, FP64 Rayleigh-quotient and residual refinement of the Ritz pairs.
+DavidsonOut davidson_mixed(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs);
 
 }  // namespace qkg

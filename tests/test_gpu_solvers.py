@@ -173,3 +173,24 @@ def test_lanczos_from_given_start_matches_oracle(qk, oracle):
                                 None, None)
     assert abs(r.energy - e.value) <= E0_RTOL * abs(e.value)
     assert abs(abs(np.vdot(r.eigenvector, evec)) - 1) < 1e-8
+
+
+@pytest.mark.parametrize("model", ["heis", "hub"])
+def test_davidson_mixed_vs_fp64(qk, model):
+    # mixed form: FP32 vectors and SpMV, FP64-accurate projections, FP64-refined
+    # Ritz pairs; its eigenvalues agree with the FP64 form's to well below the
+    # FP32 residual (error ~ residual^2 / gap)
+    if model == "heis":
+        b, s, o = make_model(qk, M.SPIN, 14, M.sector(sz2=0), M.heisenberg_terms(14, True, Jz=0.9))
+    else:
+        b, s, o = make_model(qk, M.HUBBARD, 6, M.sector(nup=3, ndn=2), M.hubbard_terms(6, False, U=3.0))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    r64 = qk.davidson_lowest_ex(H, n_eig=2, max_subspace=24, tol=1e-8, mixed=False)
+    assert r64.converged and np.all(r64.residuals <= 1e-8)
+    r32 = qk.davidson_lowest_ex(H, n_eig=2, max_subspace=24, tol=1e-5, mixed=True, return_vectors=True)
+    assert r32.converged, r32.residuals
+    assert np.all(r32.residuals <= 1e-5)
+    np.testing.assert_allclose(r32.eigenvalues, r64.eigenvalues, rtol=0, atol=1e-8)
+    for lam, v, res in zip(r32.eigenvalues, r32.eigenvectors, r32.residuals):
+        assert abs(np.linalg.norm(v) - 1) < 1e-12
+        np.testing.assert_allclose(np.linalg.norm(H.apply(v) - lam * v), res, rtol=1e-6, atol=1e-12)
