@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-ftlm", action="store_true", help="skip the batched FTLM measurement")
     p.add_argument("--no-cf", action="store_true", help="skip the batched S(q, omega) measurement")
+    p.add_argument("--no-davidson", action="store_true", help="skip the Hubbard Davidson measurement")
     p.add_argument("--cpu-sample-rows", type=int, default=1 << 19)
     return p.parse_args()
 
@@ -309,6 +310,8 @@ def main():
         out["ftlm"] = ftlm_batch(qk, args.seed, hbm_peak, peak_kind)
     if not args.no_cf:
         out["cf"] = cf_batch(qk, hbm_peak, peak_kind)
+    if not args.no_davidson:
+        out["davidson"] = davidson_hubbard(qk)
     if ws == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.cpu_sample_rows, os.cpu_count() or 1)
     print(json.dumps(out), flush=True)
@@ -410,6 +413,36 @@ def cf_batch(qk, hbm_peak, peak_kind):
                          "frac": achieved / hbm_peak, "algorithmic_bytes_per_launch": alg,
                          "launch_ms": st32["spmv_ms"]},
             "mixed_vs_fp64_max_rel_dS": float(np.abs(S32 - S64).max() / np.abs(S64).max())}
+
+
+DAV_L, DAV_K, DAV_SUB, DAV_TOL, DAV_ITERS = 16, 4, 32, 1e-8, 14
+
+
+def davidson_hubbard(qk):
+    """Davidson on the Fermi-Hubbard chain L=16 periodic, t=1, U=4,
+    N_up = N_dn = 8 (dim 165,636,900): lowest 4 eigenpairs, subspace <= 32,
+    4 corrections per iteration, tol 1e-8, the reference's algorithm.  The
+    reference runs at most 100 iterations and does not reach 1e-8 on this
+    problem; the bench times the first 14 iterations (two restart cycles) of
+    each form and reports seconds per iteration."""
+    import models as M
+    from conftest import make_model
+    b, s, o = make_model(qk, M.HUBBARD, DAV_L, M.sector(nup=DAV_L // 2, ndn=DAV_L // 2), M.hubbard_terms(DAV_L, True))
+    t0 = time.perf_counter()
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    t_build = time.perf_counter() - t0
+    res = {}
+    for mixed in (True, False):
+        r = qk.davidson_lowest_ex(H, n_eig=DAV_K, max_subspace=DAV_SUB, tol=DAV_TOL, mixed=mixed, max_iter=DAV_ITERS)
+        res[mixed] = r
+    r32, r64 = res[True], res[False]
+    return {"workload": f"hubbard_chain_L{DAV_L}_pbc_U4_half_filling_k{DAV_K}_sub{DAV_SUB}_{DAV_ITERS}_iterations",
+            "dim": H.dimension, "construct_s": t_build, "iterations": DAV_ITERS,
+            "mixed_s_per_iter": r32.seconds / r32.iterations, "fp64_s_per_iter": r64.seconds / r64.iterations,
+            "mixed_evals": [float(x) for x in r32.eigenvalues], "fp64_evals": [float(x) for x in r64.eigenvalues],
+            "mixed_residuals_fp64": [float(x) for x in r32.residuals],
+            "fp64_residuals": [float(x) for x in r64.residuals],
+            "form": "mixed: FP32 vectors and SpMV, compensated FP64-accurate projections, FP64-refined Ritz pairs"}
 
 
 def _cudart():

@@ -239,11 +239,12 @@ int qkrylov_davidson_lowest_complex_f64(qkrylov_hamiltonian_h h, int n_eig, int 
 /* Davidson with its diagnostics, in either form: mixed == 0 is the FP64
  * drop-in above; mixed != 0 keeps the Krylov vectors and the SpMV in FP32 with
  * FP64-accurate (compensated) projections and norms, and refines the returned
- * Ritz pairs in FP64 (Rayleigh quotient, residual).  residuals (optional,
- * n_eig): ||H v - lambda v|| of the returned pairs; seconds (optional): wall
- * time of the solve. */
+ * Ritz pairs in FP64 (Rayleigh quotient, residual).  max_iter: the
+ * reference's 100 iterations, or fewer (1..100).  residuals (optional, n_eig):
+ * ||H v - lambda v|| of the returned pairs; seconds (optional): wall time of
+ * the solve. */
 int qkrylov_davidson_lowest_ex(qkrylov_hamiltonian_h h, int n_eig, int max_subspace, double tol, int mixed,
-                               double* eigenvalues, double* eigenvectors, double* residuals,
+                               int max_iter, double* eigenvalues, double* eigenvectors, double* residuals,
                                qkrylov_davidson_result_c_t* result_info, double* seconds);
 
 int    qkrylov_continued_fraction_coeffs_complex_f64(qkrylov_hamiltonian_h h, const double* phi0_complex, int n_iter,

@@ -129,7 +129,7 @@ _SIGS = {
     "qkrylov_hamiltonian_select_kernel": (_i, [_vp, _i, _ip]),
     "qkrylov_hamiltonian_tuning": (_i, [_vp, _i, _ip, _dp]),
     "qkrylov_basis_states": (_i, [_vp, _u64, _u64, _u64p]),
-    "qkrylov_davidson_lowest_ex": (_i, [_vp, _i, _i, _d, _i, _dp, _dp, _dp, _vp, _dp]),
+    "qkrylov_davidson_lowest_ex": (_i, [_vp, _i, _i, _d, _i, _i, _dp, _dp, _dp, _vp, _dp]),
     "qkrylov_hamiltonian_benchmark_apply": (_i, [_vp, _i, _i, _dp]),
 }
 
@@ -478,7 +478,7 @@ class DavidsonResult:
         return f"DavidsonResult(energies={self.eigenvalues})"
 
 
-def davidson_lowest_ex(H, n_eig=1, max_subspace=20, tol=1e-8, mixed=False, return_vectors=False):
+def davidson_lowest_ex(H, n_eig=1, max_subspace=20, tol=1e-8, mixed=False, return_vectors=False, max_iter=100):
     """Davidson (davidson.cpp:86-227) in the FP64 form or the mixed form (FP32
     vectors and SpMV, FP64-accurate projections, FP64-refined Ritz pairs).
     Returns a DavidsonResult with ``residuals`` and ``seconds`` set."""
@@ -490,7 +490,7 @@ def davidson_lowest_ex(H, n_eig=1, max_subspace=20, tol=1e-8, mixed=False, retur
     info = DavidsonResultC()
     sec = _c.c_double()
     _check(lib().qkrylov_davidson_lowest_ex(H._h, int(n_eig), int(max_subspace), float(tol), int(bool(mixed)),
-                                            _dptr(ev), _dptr(vecs.view(_np.float64)) if return_vectors else None,
+                                            int(max_iter), _dptr(ev), _dptr(vecs.view(_np.float64)) if return_vectors else None,
                                             _dptr(res), _c.byref(info), _c.byref(sec)))
     r = DavidsonResult(ev[:k], list(vecs[:k]) if return_vectors else None, info.iterations, bool(info.converged))
     r.residuals, r.seconds = res[:k], sec.value

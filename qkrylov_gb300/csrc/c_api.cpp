@@ -577,13 +577,14 @@ int qkrylov_davidson_lowest_complex_f64(qkrylov_hamiltonian_h h, int n_eig, int 
     });
 }
 
-int qkrylov_davidson_lowest_ex(qkrylov_hamiltonian_h h, int n_eig, int max_sub, double tol, int mixed, double* evals,
-                               double* evecs, double* residuals, qkrylov_davidson_result_c_t* info, double* seconds) {
-    if (!h || !h->ptr || !evals || n_eig <= 0) return QKRYLOV_ERROR_INVALID_ARG;
+int qkrylov_davidson_lowest_ex(qkrylov_hamiltonian_h h, int n_eig, int max_sub, double tol, int mixed, int max_iter,
+                               double* evals, double* evecs, double* residuals, qkrylov_davidson_result_c_t* info,
+                               double* seconds) {
+    if (!h || !h->ptr || !evals || n_eig <= 0 || max_iter < 1 || max_iter > 100) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         set_device(h);
-        const auto res = mixed ? qkg::davidson_mixed(*h->ptr, n_eig, max_sub, tol, evecs != nullptr)
-                               : qkg::davidson_f64(*h->ptr, n_eig, max_sub, tol, evecs != nullptr);
+        const auto res = mixed ? qkg::davidson_mixed(*h->ptr, n_eig, max_sub, tol, evecs != nullptr, max_iter)
+                               : qkg::davidson_f64(*h->ptr, n_eig, max_sub, tol, evecs != nullptr, false, max_iter);
         const size_t k = std::min<size_t>((size_t)n_eig, res.evals.size());
         for (size_t i = 0; i < k; ++i) evals[i] = res.evals[i];
         if (residuals)

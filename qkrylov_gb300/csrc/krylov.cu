@@ -252,6 +252,67 @@ __global__ void mdot_kernel(const T2* const* __restrict__ V, int k, const T2* __
     }
 }
 
+// FP32 projections <V_j, w> (compensated) for a group of up to KB32 vectors per
+// block column, two consecutive elements per thread and iteration (16-byte
+// loads when every vector of the group and w are 16-byte aligned).
+constexpr int KB32 = 8;
+__device__ __forceinline__ void ff_cmac(FF& re, FF& im, float ax, float ay, float bx, float by) {
+    ff_add_prod(re, ax, bx);
+    ff_add_prod(re, ay, by);
+    ff_add_prod(im, ax, by);
+    ff_add_prod(im, -ay, bx);
+}
+__global__ void __launch_bounds__(kThreads) mdot32_kernel(const float2* const* __restrict__ V, int k,
+                                                          const float2* __restrict__ w, uint64_t n, double2* part,
+                                                          int stride) {
+    const int j0 = blockIdx.y * KB32;
+    const int kk = min(KB32, k - j0);
+    FF re[KB32], im[KB32];
+    const float2* vp[KB32];
+    bool al = (reinterpret_cast<uintptr_t>(w) & 15u) == 0;
+#pragma unroll
+    for (int q = 0; q < KB32; ++q) {
+        re[q] = im[q] = FF{0.f, 0.f};
+        vp[q] = V[j0 + (q < kk ? q : 0)];
+        al = al && (reinterpret_cast<uintptr_t>(vp[q]) & 15u) == 0;
+    }
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    uint64_t done = 0;
+    if (al) {
+        const uint64_t n2 = n / 2;
+        const float4* w4 = reinterpret_cast<const float4*>(w);
+        for (uint64_t i = t0; i < n2; i += step) {
+            const float4 b = w4[i];
+#pragma unroll
+            for (int q = 0; q < KB32; ++q) {
+                if (q < kk) {
+                    const float4 a = reinterpret_cast<const float4*>(vp[q])[i];
+                    ff_cmac(re[q], im[q], a.x, a.y, b.x, b.y);
+                    ff_cmac(re[q], im[q], a.z, a.w, b.z, b.w);
+                }
+            }
+        }
+        done = 2 * n2;
+    }
+    for (uint64_t i = done + t0; i < n; i += step) {
+        const float2 b = w[i];
+#pragma unroll
+        for (int q = 0; q < KB32; ++q)
+            if (q < kk) {
+                const float2 a = vp[q][i];
+                ff_cmac(re[q], im[q], a.x, a.y, b.x, b.y);
+            }
+    }
+#pragma unroll
+    for (int q = 0; q < KB32; ++q) {
+        if (q < kk) {
+            const double2 s = block_sum(make_double2(ff_value(re[q]), ff_value(im[q])));
+            if (threadIdx.x == 0) part[(size_t)(j0 + q) * stride + blockIdx.x] = s;
+        }
+    }
+}
+
 // w += sum_j c_j V_j ; coefficients (complex double) in global memory.
 template <class T2, class A>
 __global__ void mcomb_kernel(const T2* const* __restrict__ V, int k, const double2* __restrict__ c, T2* __restrict__ w,
@@ -447,8 +508,14 @@ static void mdot_impl(const T2* const* V, int k, const T2* w, uint64_t n, std::c
     int g = stream_grid(n);
     g = (int)std::min<size_t>((size_t)g, ws.cap_partials / (size_t)k);
     g = std::max(1, g);
-    dim3 grid(g, (k + KB - 1) / KB);
-    mdot_kernel<T2, F32><<<grid, kThreads, 0, s>>>(V, k, w, n, ws.partial.as<double2>(), g);
+    if (F32) {
+        dim3 grid(g, (k + KB32 - 1) / KB32);
+        mdot32_kernel<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float2* const*>(V), k,
+                                                reinterpret_cast<const float2*>(w), n, ws.partial.as<double2>(), g);
+    } else {
+        dim3 grid(g, (k + KB - 1) / KB);
+        mdot_kernel<T2, F32><<<grid, kThreads, 0, s>>>(V, k, w, n, ws.partial.as<double2>(), g);
+    }
     QKG_LAUNCHED();
     const double2* r = finish(ws, g, g, k, s);
     for (int j = 0; j < k; ++j) out[j] = {r[j].x, r[j].y};

@@ -640,7 +640,8 @@ template <> struct DavOps<float2> {
 // and norms by compensated reductions in FP64, corrections orthogonalised twice,
 // and the final Ritz pairs refined in FP64 (Rayleigh quotient, residual).
 template <class T2>
-DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream) {
+DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream,
+                          int max_iter) {
     using Op = DavOps<T2>;
     constexpr bool MIXED = std::is_same<T2, float2>::value;
     DavidsonOut out;
@@ -711,7 +712,7 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
     for (auto& r : rbuf) r.alloc(n * sizeof(T2));
     std::vector<T2*> rptr;
     for (auto& r : rbuf) rptr.push_back(r.as<T2>());
-    for (int iter = 0; iter < 100; ++iter) {
+    for (int iter = 0; iter < max_iter; ++iter) {
         const int m = (int)V.size();
         for (int i = (int)rows.size(); i < m; ++i) {
             std::vector<cd> col(i + 1);
@@ -754,7 +755,7 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
                 corr.push_back(std::move(t));
             }
         }
-        if (all_conv || iter == 99) {
+        if (all_conv || iter == max_iter - 1) {
             out.iters = iter + 1;
             out.converged = all_conv;
             out.evals.assign(ev.begin(), ev.begin() + n_eig);
@@ -836,11 +837,12 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
 }
 }  // namespace
 
-DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream) {
-    return davidson_impl<double2>(H, n_eig, max_sub, tol, want_vecs, f32_stream);
+DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream,
+                         int max_iter) {
+    return davidson_impl<double2>(H, n_eig, max_sub, tol, want_vecs, f32_stream, max_iter);
 }
-DavidsonOut davidson_mixed(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs) {
-    return davidson_impl<float2>(H, n_eig, max_sub, tol, want_vecs, false);
+DavidsonOut davidson_mixed(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, int max_iter) {
+    return davidson_impl<float2>(H, n_eig, max_sub, tol, want_vecs, false, max_iter);
 }
 
 }  // namespace qkg

@@ -132,9 +132,12 @@ struct DavidsonOut {
     std::vector<double> residuals;  // ||H v - lambda v|| of the returned pairs (FP64 for the mixed form)
     double seconds = 0.0;
 };
-DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream = false);
+// max_iter: the reference's fixed 100 iterations (davidson.cpp:141,180) unless
+// a caller asks for fewer (timing runs).
+DavidsonOut davidson_f64(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, bool f32_stream = false,
+                         int max_iter = 100);
 // Mixed form: FP32 Krylov vectors and SpMV, FP64-accurate (compensated) projections
 // and norms, FP64 Rayleigh-quotient and residual refinement of the Ritz pairs.
-DavidsonOut davidson_mixed(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs);
+DavidsonOut davidson_mixed(Hamiltonian& H, int n_eig, int max_sub, double tol, bool want_vecs, int max_iter = 100);
 
 }  // namespace qkg
