@@ -28,10 +28,11 @@ constexpr int kT = 256;
 constexpr int kUpdGrid = 152 * 8;
 constexpr int kTimedSteps = 8;  // steps launched one by one with an SpMV timer before the graph takes over
 constexpr int kInFlight = 6;    // steps the host lets the GPU run ahead of its checks
+constexpr double kOrthTol = 3.4526698300124393e-4;  // sqrt(2^-23): FP32 semiorthogonality level
 
 struct LzState {
     int k;
-    int pad;
+    int orth;               // this step's correction along the Ritz vector is applied
     double a, b;            // update coefficients of the current step
     double pre, pim;        // projection on the Ritz vector (selective reorthogonalisation)
 };
@@ -105,36 +106,67 @@ __global__ void lz_update_kernel(void* const* __restrict__ vtab, const LzState* 
     if (threadIdx.x == 0) bpart[blockIdx.x] = s;
 }
 
-// <psi, W> partials (complex) for selective reorthogonalisation.
-__global__ void lz_proj_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st,
-                               const float2* __restrict__ psi, uint64_t n, double2* __restrict__ ppart) {
-    const float2* __restrict__ w = static_cast<const float2*>(vtab[st->k + 1]);
-    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+// The update of lz_update_kernel fused with the partials of <psi, W>
+// (selective reorthogonalisation): one pass over W, v, v_prev and psi.
+__global__ void lz_update_proj_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st, uint64_t n,
+                                      const float2* __restrict__ psi, double2* __restrict__ bpart,
+                                      double2* __restrict__ ppart) {
+    const int k = st->k;
+    float2* __restrict__ w = static_cast<float2*>(vtab[k + 1]);
+    const float2* __restrict__ v = static_cast<const float2*>(vtab[k]);
+    const float2* __restrict__ vp = k > 0 ? static_cast<const float2*>(vtab[k - 1]) : nullptr;
+    const float a = (float)st->a, b = (float)st->b;
+    float hi = 0.f, lo = 0.f, rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const float2 a = psi[i], b = w[i];
-        ff_acc(rh, rl, a.x, b.x);
-        ff_acc(rh, rl, a.y, b.y);
-        ff_acc(ih, il, a.x, b.y);
-        ff_acc(ih, il, -a.y, b.x);
+        float2 x = w[i];
+        const float2 c = v[i];
+        x.x = fmaf(-a, c.x, x.x);
+        x.y = fmaf(-a, c.y, x.y);
+        if (vp) {
+            const float2 d = vp[i];
+            x.x = fmaf(-b, d.x, x.x);
+            x.y = fmaf(-b, d.y, x.y);
+        }
+        w[i] = x;
+        ff_acc(hi, lo, x.x, x.x);
+        ff_acc(hi, lo, x.y, x.y);
+        const float2 p = psi[i];
+        ff_acc(rh, rl, p.x, x.x);
+        ff_acc(rh, rl, p.y, x.y);
+        ff_acc(ih, il, p.x, x.y);
+        ff_acc(ih, il, -p.y, x.x);
     }
-    const double2 s = bsum2((double)rh + (double)rl, (double)ih + (double)il);
-    if (threadIdx.x == 0) ppart[blockIdx.x] = s;
+    const double2 s = bsum2((double)hi + (double)lo, 0.0);
+    const double2 q = bsum2((double)rh + (double)rl, (double)ih + (double)il);
+    if (threadIdx.x == 0) {
+        bpart[blockIdx.x] = s;
+        ppart[blockIdx.x] = q;
+    }
 }
-__global__ void lz_proj_finish_kernel(const double2* __restrict__ ppart, int nparts, LzState* st) {
-    double r = 0.0, i = 0.0;
+
+// c = <psi, W>; the correction is applied only when |c| exceeds orth_tol ||W||
+// (components below the square root of the working precision are harmless,
+// Parlett & Scott 1979), so most steps skip the extra pass over W.
+__global__ void lz_proj_finish_kernel(const double2* __restrict__ ppart, const double2* __restrict__ bpart,
+                                      int nparts, LzState* st, double orth_tol) {
+    double r = 0.0, i = 0.0, w2 = 0.0;
     for (int j = threadIdx.x; j < nparts; j += blockDim.x) {
         r += ppart[j].x;
         i += ppart[j].y;
+        w2 += bpart[j].x;
     }
     const double2 t = bsum2(r, i);
+    const double2 u = bsum2(w2, 0.0);
     if (threadIdx.x == 0) {
         st->pre = t.x;
         st->pim = t.y;
+        st->orth = (t.x * t.x + t.y * t.y) > orth_tol * orth_tol * u.x ? 1 : 0;
     }
 }
 // W -= c psi with c = <psi, W>; |W|^2 partials.
 __global__ void lz_orth_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st,
                                const float2* __restrict__ psi, uint64_t n, double2* __restrict__ bpart) {
+    if (!st->orth) return;  // bpart keeps the partials of the unchanged W
     float2* __restrict__ w = static_cast<float2*>(vtab[st->k + 1]);
     const float cr = (float)st->pre, ci = (float)st->pim;
     float hi = 0.f, lo = 0.f;
@@ -196,13 +228,10 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     const size_t need = (size_t)(nmax + 1) * n * sizeof(float2);
     if (need + (512ull << 20) > fr)
         throw Error(CUDA_ERR, "out of device memory for " + std::to_string(nmax + 1) + " Krylov vectors");
-    std::vector<DBuf> V;
-    V.reserve(nmax + 1);
+    // one allocation for all vectors (a cudaMalloc per vector costs more than a step)
+    DBuf V((size_t)(nmax + 1) * n * sizeof(float2));
     std::vector<void*> vptr;
-    for (int i = 0; i <= nmax; ++i) {
-        V.emplace_back(n * sizeof(float2));
-        vptr.push_back(V.back().p);
-    }
+    for (int i = 0; i <= nmax; ++i) vptr.push_back(V.as<float2>() + (size_t)i * n);
     DBuf vtab((nmax + 1) * sizeof(void*));
     QKG_CUDA(cudaMemcpy(vtab.p, vptr.data(), vptr.size() * sizeof(void*), cudaMemcpyHostToDevice));
     DBuf state(sizeof(LzState)), alpha((nmax + 2) * 8), beta((nmax + 2) * 8), sig((nmax + 2) * 8);
@@ -249,14 +278,16 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
         lz_alpha_kernel<<<1, kT, 0, st>>>(apart.as<double2>(), nparts, state.as<LzState>(), alpha.as<double>(),
                                           beta.as<double>(), sig.as<double>(), ah.d);
         QKG_LAUNCHED();
-        lz_update_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
-                                                  bpart.as<double2>());
-        QKG_LAUNCHED();
-        if (so) {
-            lz_proj_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(),
-                                                    psi.as<float2>(), n, ppart.as<double2>());
+        if (!so) {
+            lz_update_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
+                                                      bpart.as<double2>());
             QKG_LAUNCHED();
-            lz_proj_finish_kernel<<<1, kT, 0, st>>>(ppart.as<double2>(), kUpdGrid, state.as<LzState>());
+        } else {
+            lz_update_proj_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
+                                                           psi.as<float2>(), bpart.as<double2>(), ppart.as<double2>());
+            QKG_LAUNCHED();
+            lz_proj_finish_kernel<<<1, kT, 0, st>>>(ppart.as<double2>(), bpart.as<double2>(), kUpdGrid,
+                                                    state.as<LzState>(), kOrthTol);
             QKG_LAUNCHED();
             lz_orth_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(),
                                                     psi.as<float2>(), n, bpart.as<double2>());
@@ -278,7 +309,7 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
         QKG_CUDA(cudaGraphDestroy(g));
         return ge;
     };
-    const int kernels_plain = 4, kernels_so = 7;
+    const int kernels_plain = 4, kernels_so = 6;
     cudaGraphExec_t g_plain = nullptr, g_so = nullptr;
     std::vector<cudaEvent_t> ev(kInFlight + 2);
     for (auto& e : ev) QKG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
