@@ -285,7 +285,8 @@ def main():
     achieved = alg_bytes / spmv_s / 1e9
     tr = profile_traffic()
     variant, _ = H.tuning(fp32=True)
-    kname = {"rows4": "spmv_rows_kernel<float>", "row": "spmv_fast_kernel<float>",
+    kname = {"rows4": "spmv_rows_kernel<float>", "rows4_staged": "spmv_rows_kernel<float, staged>",
+             "row": "spmv_fast_kernel<float>",
              "staged": "spmv_fast_kernel<float, staged>"}.get(variant, "spmv_kernel<float>")
     out["roofline"] = {"kernel": kname + " (FP32 SpMV)", "bound": "hbm", "achieved": achieved,
                        "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,

@@ -30,8 +30,9 @@ struct DBuf {
 enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
 
 // Fast SpMV kernel variants: one row per thread, the outer block's slice of x
-// staged in shared memory, four rows per thread.
-enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2 };
+// staged in shared memory, four rows per thread, four rows per thread with the
+// block staged.
+enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3 };
 
 // Device-resident Lanczos step: the SpMV reads its vectors through a device
 // pointer table indexed by a device step counter (x = vtab[k], y = vtab[k+1]),
@@ -100,7 +101,7 @@ public:
     bool fast() const { return fast_ && !force_generic_; }
     // kernel mode: 0 automatic (autotuned), 1 generic kernel, 2 fast kernel
     // one row per thread, 3 fast kernel with shared-memory staging, 4 fast
-    // kernel four rows per thread
+    // kernel four rows per thread, 5 four rows per thread with staging
     void set_kernel_mode(int m) { mode_ = m; force_generic_ = (m == 1); }
     void force_generic(bool on) { set_kernel_mode(on ? 1 : 0); }
     // fast-kernel variant for vectors of elem_bytes per element
@@ -109,10 +110,15 @@ public:
         if (mode_ == 2) return FV_ROW;
         if (mode_ == 3) return can_stage ? FV_STAGED : FV_ROW;
         if (mode_ == 4) return FV_ROWS4;
+        if (mode_ == 5) return can_stage ? FV_ROWS4_STAGED : FV_ROWS4;
         const FastVariant v = pref_[elem_bytes == 16 ? 1 : 0];
-        return (v == FV_STAGED && !can_stage) ? FV_ROW : v;
+        if (v == FV_STAGED && !can_stage) return FV_ROW;
+        if (v == FV_ROWS4_STAGED && !can_stage) return FV_ROWS4;
+        return v;
     }
-    bool staged(size_t elem_bytes) const { return fast() && variant(elem_bytes) == FV_STAGED; }
+    bool staged(size_t elem_bytes) const {
+        return fast() && (variant(elem_bytes) == FV_STAGED || variant(elem_bytes) == FV_ROWS4_STAGED);
+    }
     // autotuner record: mean ms of [precision][variant] (0 when not measured)
     double tuned_ms(int prec, int v) const { return tune_ms_[prec][v]; }
     size_t inner_table_entries() const { return n_ient_; }
@@ -140,7 +146,7 @@ private:
     bool fast_ = false, force_generic_ = false, unif_ = false;
     int mode_ = 0;
     FastVariant pref_[2] = {FV_ROWS4, FV_ROWS4};
-    double tune_ms_[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    double tune_ms_[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     DBuf items_blk_;            // one work item per outer block (staged kernel)
     size_t n_items_blk_ = 0, max_block_ = 0;
     double u_ar_ = 0.0, u_ai_ = 0.0;

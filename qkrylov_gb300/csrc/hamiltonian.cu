@@ -429,11 +429,13 @@ static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread
 #ifndef QKG_ELL_PREFETCH
 #define QKG_ELL_PREFETCH 1
 #endif
-template <class T, class A, bool REAL, bool UNIF, bool OJ>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
+template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE>
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (STAGE ? QKG_ROWS_MINB - 1 : QKG_ROWS_MINB) : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
                                                            typename V2<T>::t* __restrict__ y_in) {
     using T2 = typename V2<T>::t;
     constexpr int RT = kRowsPerThread;
+    extern __shared__ __align__(16) unsigned char rows_smem[];
+    T2* xs = reinterpret_cast<T2*>(rows_smem);  // STAGE: the outer block's slice of x
     const T2* __restrict__ x = x_in;
     T2* __restrict__ y = y_in;
     A scale = (A)1;
@@ -456,6 +458,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_R
     const KTerm<uint32_t, A>* mixed = mixed_smem ? s_mixed : p.mixed;
     const WorkItem it = p.items[blockIdx.x];
     const uint32_t block_off = __ldg(p.outer_off + it.a);
+    if (STAGE)  // the item is the whole outer block: rows [block_off, block_off + count)
+        for (uint32_t i = threadIdx.x; i < it.count; i += blockDim.x) xs[i] = x[block_off + i];
     if (!UNIF) {
         const uint32_t sa = it.a << p.n_in;
         for (int t = threadIdx.x; t < p.n_inner; t += blockDim.x) {
@@ -496,13 +500,16 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_R
     const int nout = s_n;
     const uint32_t rmask = (1u << p.rbits) - 1u;
 
+    A dot_hi = 0, dot_lo = 0;
+    // passes of kChunk rows (one pass unless a whole outer block is staged)
+    for (uint32_t pass = 0; pass < (STAGE ? it.count : 1u); pass += kChunk) {
     uint32_t s[RT], e0[RT], e1[RT];
     A ar_[RT], ai_[RT];
     bool live[RT];
-    const T2* xr = x + (uint32_t)it.row0 + threadIdx.x;  // row q of this thread is xr[q * kBlock]
+    const T2* xr = x + (uint32_t)it.row0 + pass + threadIdx.x;  // row q of this thread is xr[q * kBlock]
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
-        const uint32_t r = threadIdx.x + q * kBlock;
+        const uint32_t r = pass + threadIdx.x + q * kBlock;
         live[q] = r < it.count;
         const uint32_t rr = live[q] ? r : 0;
         const uint32_t pidx = it.inner_base + rr;
@@ -545,7 +552,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_R
         for (int q = 0; q < RT; ++q) {
             e0[q] += 32;
             nxt[q] = (cur[q] != kEllEmpty && e0[q] < e1[q]) ? __ldg(p.ient + e0[q]) : kEllEmpty;
-            if (cur[q] != kEllEmpty) xv[q] = x[block_off + (cur[q] & rmask)];
+            if (cur[q] != kEllEmpty) xv[q] = STAGE ? xs[cur[q] & rmask] : x[block_off + (cur[q] & rmask)];
         }
         more = false;
 #pragma unroll
@@ -580,7 +587,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_R
         T2 xv[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q)
-            if (ent[q] != kEllEmpty) xv[q] = x[block_off + (ent[q] & rmask)];
+            if (ent[q] != kEllEmpty) xv[q] = STAGE ? xs[ent[q] & rmask] : x[block_off + (ent[q] & rmask)];
 #pragma unroll
         for (int q = 0; q < RT; ++q) {
             if (ent[q] == kEllEmpty) {
@@ -619,15 +626,15 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_R
             cmac<A>(ar_[q], ai_[q], cr, ci, x[idx], REAL);
         }
     }
-    A dot_hi = 0, dot_lo = 0;
     T2 xd[RT];
     uint32_t dc[RT];
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
-        const uint32_t row = (uint32_t)it.row0 + (live[q] ? threadIdx.x + q * kBlock : 0u);
+        const uint32_t rl = live[q] ? pass + threadIdx.x + q * kBlock : 0u;
+        const uint32_t row = (uint32_t)it.row0 + rl;
         dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
                                        : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
-        xd[q] = x[row];
+        xd[q] = STAGE ? xs[rl] : x[row];
     }
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
@@ -643,11 +650,12 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? QKG_ROWS_MINB : QKG_R
         T2 out;
         out.x = (T)(accr * scale);
         out.y = (T)(acci * scale);
-        y[(uint32_t)it.row0 + threadIdx.x + q * kBlock] = out;
+        y[(uint32_t)it.row0 + pass + threadIdx.x + q * kBlock] = out;
         if (p.apart) {
             ffma_acc(dot_hi, dot_lo, (A)xd[q].x, (A)out.x);
             ffma_acc(dot_hi, dot_lo, (A)xd[q].y, (A)out.y);
         }
+    }
     }
     if (p.apart) {
         const double sum = block_sum_d((double)dot_hi + (double)dot_lo);
@@ -989,9 +997,9 @@ void Hamiltonian::autotune() {
         QKG_CUDA(cudaEventCreate(&a));
         QKG_CUDA(cudaEventCreate(&b));
         double best = 0.0;
-        for (int v = 0; v < 3; ++v) {
-            if (v == FV_STAGED && !(max_block_ * e <= kStageLimit)) continue;
-            mode_ = v == FV_ROW ? 2 : v == FV_STAGED ? 3 : 4;
+        for (int v = 0; v < 4; ++v) {
+            if ((v == FV_STAGED || v == FV_ROWS4_STAGED) && !(max_block_ * e <= kStageLimit)) continue;
+            mode_ = v == FV_ROW ? 2 : v == FV_STAGED ? 3 : v == FV_ROWS4 ? 4 : 5;
             auto run = [&] {
                 if (prec) apply_f64(x.as<double2>(), y.as<double2>(), stream_);
                 else apply_f32(x.as<float2>(), y.as<float2>(), stream_);
@@ -1070,16 +1078,25 @@ static void launch_fast(const FastParams<A>& p, size_t n_items, bool real, bool 
     const unsigned g = (unsigned)n_items;
     const int key = (var == FV_STAGED ? 8 : 0) | (real ? 4 : 0) | (unif ? 2 : 0) | (outer_has_j ? 1 : 0);
     const size_t sm = stage_smem;
-    if (var == FV_ROWS4) {
-        switch (key) {
-            case 0: spmv_rows_kernel<T, A, false, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 1: spmv_rows_kernel<T, A, false, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 2: spmv_rows_kernel<T, A, false, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 3: spmv_rows_kernel<T, A, false, true, true><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 4: spmv_rows_kernel<T, A, true, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 5: spmv_rows_kernel<T, A, true, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 6: spmv_rows_kernel<T, A, true, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
-            default: spmv_rows_kernel<T, A, true, true, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+    if (var == FV_ROWS4 || var == FV_ROWS4_STAGED) {
+        const bool st = var == FV_ROWS4_STAGED;
+        switch ((st ? 8 : 0) | (key & 7)) {
+            case 0: spmv_rows_kernel<T, A, false, false, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 1: spmv_rows_kernel<T, A, false, false, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 2: spmv_rows_kernel<T, A, false, true, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 3: spmv_rows_kernel<T, A, false, true, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 4: spmv_rows_kernel<T, A, true, false, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 5: spmv_rows_kernel<T, A, true, false, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 6: spmv_rows_kernel<T, A, true, true, false, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 7: spmv_rows_kernel<T, A, true, true, true, false><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 8: spmv_rows_kernel<T, A, false, false, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            case 9: spmv_rows_kernel<T, A, false, false, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            case 10: spmv_rows_kernel<T, A, false, true, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            case 11: spmv_rows_kernel<T, A, false, true, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            case 12: spmv_rows_kernel<T, A, true, false, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            case 13: spmv_rows_kernel<T, A, true, false, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            case 14: spmv_rows_kernel<T, A, true, true, false, true><<<g, kBlock, sm, s>>>(p, x, y); break;
+            default: spmv_rows_kernel<T, A, true, true, true, true><<<g, kBlock, sm, s>>>(p, x, y); break;
         }
         QKG_LAUNCHED();
         return;
@@ -1117,6 +1134,14 @@ static void allow_stage_smem(size_t bytes) {
     QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, true, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, false, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, false, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, false, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
 }
 
 Hamiltonian::~Hamiltonian() {
@@ -1233,7 +1258,7 @@ static void launch_spmv(const DevBasis& b, const TermSet& ts, const DBuf& items,
 void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const {
     if (fast()) {
         const FastVariant v = variant(16);
-        const bool st = v == FV_STAGED;
+        const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
         FastParams<double> p;
         fast_params(p);
         if (st) p.items = items_blk_.as<WorkItem>();
@@ -1251,7 +1276,7 @@ void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const 
 void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) const {
     QKG_REQUIRE(fast(), "the device-resident Lanczos step needs the fast SpMV kernel");
     const FastVariant v = variant(8);
-    const bool st = v == FV_STAGED;
+    const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
     FastParams<float> p;
     fast_params(p);
     if (st) p.items = items_blk_.as<WorkItem>();
@@ -1263,12 +1288,16 @@ void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) cons
                               st ? max_block_ * 8 : 0);
 }
 
-size_t Hamiltonian::lanczos_parts() const { return staged(8) ? n_items_blk_ : n_items_; }
+size_t Hamiltonian::lanczos_parts() const {
+    if (!fast()) return n_items_;
+    const FastVariant v = variant(8);
+    return (v == FV_STAGED || v == FV_ROWS4_STAGED) ? n_items_blk_ : n_items_;
+}
 
 void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
     if (fast()) {
         const FastVariant v = variant(8);
-        const bool st = v == FV_STAGED;
+        const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
         FastParams<float> p;
         fast_params(p);
         if (st) p.items = items_blk_.as<WorkItem>();

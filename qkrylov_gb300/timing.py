@@ -49,7 +49,7 @@ def main():
     p.add_argument("--L", type=int, default=28)
     p.add_argument("--obc", action="store_true")
     p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    p.add_argument("--mode", type=int, default=0, help="0 autotuned, 1 generic, 2 fast, 3 fast staged, 4 fast rows4")
+    p.add_argument("--mode", type=int, default=0, help="0 autotuned, 1 generic, 2 fast, 3 fast staged, 4 fast rows4, 5 rows4 staged")
     p.add_argument("--reps", type=int, default=5)
     p.add_argument("--block", type=int, default=0, help="vectors per sector: batched Lanczos over all Sz sectors")
     p.add_argument("--steps", type=int, default=3)
