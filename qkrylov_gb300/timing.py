@@ -4,8 +4,9 @@ profiles are taken with).
     python -m qkrylov_gb300.timing --model heisenberg --L 28 --precision fp32 --mode 0 --reps 5
     python -m qkrylov_gb300.timing --L 22 --block 32 --steps 3 --vpl 4
 
-The second form runs the batched Lanczos on every Sz sector of the chain with
-``--block`` Philox start vectors per sector and reports the block-SpMV time.
+The second form runs the batched Lanczos on every Sz sector of the chain (or
+the Sz = 0 sector alone with ``--sz0-only``) with ``--block`` Philox start
+vectors per sector and reports the block-SpMV time.
 
 Builds the Hamiltonian (Heisenberg chain ``Sz Sz + 0.5 (S+ S- + S- S+)`` per
 bond, or Fermi-Hubbard chain ``-t c^dag c`` hopping per spin and direction plus
@@ -54,6 +55,7 @@ def main():
     p.add_argument("--block", type=int, default=0, help="vectors per sector: batched Lanczos over all Sz sectors")
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--vpl", type=int, default=0, help="block SpMV vectors per lane (0: autotuned)")
+    p.add_argument("--sz0-only", action="store_true", help="block mode on the Sz = 0 sector alone")
     a = p.parse_args()
     if a.block:
         return block(a)
@@ -75,7 +77,7 @@ def main():
 def block(a):
     t0 = time.perf_counter()
     hams = []
-    for sz2 in range(-a.L, a.L + 1, 2):
+    for sz2 in ([0] if a.sz0_only else range(-a.L, a.L + 1, 2)):
         hams.append(qk.MatrixFreeHamiltonian(*heisenberg_chain(a.L, not a.obc, sz2=sz2)))
     tc = time.perf_counter() - t0
     mixed = a.precision == "fp32"

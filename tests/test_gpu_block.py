@@ -208,3 +208,18 @@ def test_structure_factor_block(qk, oracle, mixed):
         So = np.array([spectral(oracle, a, bb, nrm, w, E0, 0.05) for w in omegas])
         tol = OBS_RTOL if not mixed else MIXED_RTOL
         assert np.abs(S[k] - So).max() <= tol * np.abs(So).max()
+
+
+def test_ftlm_sectors_host_reduction_matches(qk):
+    # the sharded path's host reduction (one rank here) against the library's
+    from qkrylov_gb300.parallel import ftlm_sectors_distributed
+    L, R, Mst = 10, 4, 20
+    betas = np.array([0.1, 1.0, 4.0])
+    hams, _ = chain_sectors(qk, L)
+    sizes = [h.dimension for h in hams]
+    Z, E, C, ls = ftlm_sectors_distributed(lambda idx: [hams[i] for i in idx], sizes, betas, n_random=R,
+                                           n_steps=Mst, mixed=False, start="ftlm")
+    r = qk.ftlm_sectors(hams, betas, n_random=R, n_steps=Mst, mixed=False, start="ftlm", shifted=True)
+    np.testing.assert_allclose(Z * np.exp(ls), r.partition_function * np.exp(r.log_shift), rtol=1e-9)
+    np.testing.assert_allclose(E, r.internal_energy, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(C, r.specific_heat, rtol=1e-8, atol=1e-8)
