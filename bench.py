@@ -221,7 +221,7 @@ def main():
         return
     import qkrylov_gb300 as qk
     import models as M
-    from conftest import make_model
+    from models import make_model
     qk.set_device(local)
     basis, site, ops = make_model(qk, M.SPIN, L_SITES, M.sector(sz2=SZ2), heis_terms())
     t0 = time.perf_counter()
@@ -328,7 +328,7 @@ def ftlm_batch(qk, seed, hbm_peak, peak_kind):
     [0.01, 10] (shifted evaluation).  Mixed form (FP32 block vectors and SpMV,
     compensated reductions in FP64) and the FP64 form on the same vectors."""
     import models as M
-    from conftest import make_model
+    from models import make_model
     hams = []
     for sz2 in range(-FTLM_L, FTLM_L + 1, 2):
         b, s, o = make_model(qk, M.SPIN, FTLM_L, M.sector(sz2=sz2), M.heisenberg_terms(FTLM_L, True))
@@ -377,7 +377,7 @@ def cf_batch(qk, hbm_peak, peak_kind):
     fractions in one batched run of 300 steps (mixed form, and FP64 for the
     comparison), S on 2000 omega in [0, 4] with eta = 0.05."""
     import models as M
-    from conftest import make_model
+    from models import make_model
     b, s, o = make_model(qk, M.SPIN, CF_L, M.sector(sz2=0), M.heisenberg_terms(CF_L, True))
     H = qk.MatrixFreeHamiltonian(b, s, o)
     t0 = time.perf_counter()
@@ -427,7 +427,7 @@ def davidson_hubbard(qk):
     problem; the bench times the first 14 iterations (two restart cycles) of
     each form and reports seconds per iteration."""
     import models as M
-    from conftest import make_model
+    from models import make_model
     b, s, o = make_model(qk, M.HUBBARD, DAV_L, M.sector(nup=DAV_L // 2, ndn=DAV_L // 2), M.hubbard_terms(DAV_L, True))
     t0 = time.perf_counter()
     H = qk.MatrixFreeHamiltonian(b, s, o)

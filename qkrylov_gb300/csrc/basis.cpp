@@ -314,6 +314,12 @@ struct Basis::DevCopy {
         for (void* p : allocs) cudaFree(p);
         if (cur != dev) cudaSetDevice(cur);
     }
+    void* alloc(size_t bytes) {
+        void* p = nullptr;
+        QKG_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
+        allocs.push_back(p);
+        return p;
+    }
     template <class T>
     const T* upload(const std::vector<T>& v) {
         if (v.empty()) return nullptr;
@@ -348,7 +354,12 @@ const DevBasis& Basis::device(int dev) {
     d.inner_rank = c->upload(inner_rank);
     d.inner_state = c->upload(inner_state);
     d.states_int = c->upload(states_int);
-    if (permuted && dim) {
+    if (permuted && dim && split && model != TJ && rank_kind == RANK_TABLE && nbits <= 64) {
+        // Hubbard: interleaved reference ranks computed on the device
+        void* p = c->alloc(dim * (d.idx32 ? sizeof(uint32_t) : sizeof(uint64_t)));
+        ref_permutation_device(d, sec, work_items(1024), p);
+        d.ref_of_int = p;
+    } else if (permuted && dim) {
         if (d.idx32) {
             std::vector<uint32_t> p(dim);
 #pragma omp parallel for schedule(static)

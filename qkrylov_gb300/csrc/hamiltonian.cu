@@ -1023,6 +1023,58 @@ void Hamiltonian::autotune() {
     mode_ = saved;
 }
 
+// Rank of each internal state in the reference's interleaved order
+// (up bit i -> bit 2i, down bit i -> bit 2i+1; the same count as
+// Basis::index_ref: for every set bit p, high to low, the valid states sharing
+// the bits above p with 0 at p).  One thread per row of a work item.
+__global__ void ref_perm_kernel(const WorkItem* __restrict__ items, const uint32_t* __restrict__ inner_state,
+                                int n_in, int N, int nbits, int use_nup, int use_ndn, int nup, int ndn,
+                                const unsigned long long* __restrict__ binom_tab, int idx32, void* out) {
+    __shared__ unsigned long long C[33 * 33];
+    for (int i = threadIdx.x; i < 33 * 33; i += blockDim.x) C[i] = binom_tab[i];
+    __syncthreads();
+    const WorkItem it = items[blockIdx.x];
+    for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
+        const uint64_t b = inner_state ? (uint64_t)__ldg(inner_state + it.inner_base + r) : (uint64_t)(it.inner_base + r);
+        const uint64_t up = b, dn = (uint64_t)it.a;  // internal state = dn << n_in | up, n_in = N
+        unsigned long long rank = 0;
+        int up_rem = nup, dn_rem = ndn;
+        for (int p = nbits - 1; p >= 0; --p) {
+            const int i = p >> 1;
+            const bool set = (p & 1) ? ((dn >> i) & 1ull) : ((up >> i) & 1ull);
+            if (!set) continue;
+            const int us = (p + 1) >> 1, ds = p >> 1;
+            const unsigned long long cu =
+                use_nup ? ((up_rem >= 0 && up_rem <= us) ? C[us * 33 + up_rem] : 0ull) : (1ull << us);
+            const unsigned long long cd =
+                use_ndn ? ((dn_rem >= 0 && dn_rem <= ds) ? C[ds * 33 + dn_rem] : 0ull) : (1ull << ds);
+            rank += cu * cd;
+            if (p & 1) --dn_rem; else --up_rem;
+        }
+        const uint64_t row = it.row0 + r;
+        if (idx32) static_cast<uint32_t*>(out)[row] = (uint32_t)rank;
+        else static_cast<unsigned long long*>(out)[row] = rank;
+    }
+    (void)n_in;
+    (void)N;
+}
+
+void ref_permutation_device(const DevBasis& d, const Sector& sec, const std::vector<WorkItem>& items, void* out) {
+    QKG_REQUIRE(d.split && d.N <= 32 && d.n_in == d.N, "device permutation: split basis with up bits inner");
+    if (items.empty()) return;
+    std::vector<unsigned long long> tab(33 * 33, 0);
+    for (int n = 0; n <= 32; ++n)
+        for (int k = 0; k <= n; ++k) tab[n * 33 + k] = binom(n, k);
+    DBuf t, it;
+    upload_vec(t, tab);
+    upload_vec(it, items);
+    ref_perm_kernel<<<(unsigned)items.size(), 256>>>(it.as<WorkItem>(), d.inner_all ? nullptr : d.inner_state, d.n_in,
+                                                     d.N, d.nbits, sec.use_nup ? 1 : 0, sec.use_ndn ? 1 : 0, sec.nup,
+                                                     sec.ndn, t.as<unsigned long long>(), d.idx32, out);
+    QKG_LAUNCHED();
+    QKG_CUDA(cudaDeviceSynchronize());
+}
+
 template <class A>
 void Hamiltonian::fast_params(FastParams<A>& p) const {
     const DevBasis& b = *db_;

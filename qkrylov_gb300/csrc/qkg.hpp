@@ -148,6 +148,10 @@ private:
 
 uint64_t binom(int n, int k);
 
+// Reference index of every internal index of a split (Hubbard) basis, computed
+// on the device from the work items (out: uint32 when idx32, else uint64).
+void ref_permutation_device(const DevBasis& d, const Sector& sec, const std::vector<WorkItem>& items, void* out);
+
 // ---------------------------------------------------------------- operators
 struct Factor { std::string op; int site; };
 struct Term { std::complex<double> coeff; std::vector<Factor> factors; };

@@ -62,21 +62,5 @@ def qk():
     return qkrylov_gb300
 
 
-def make_model(qk, model, nsites, sector, terms):
-    """Basis, site and OpSum objects of the GPU library for a model tuple."""
-    use_sz, sz2, use_nup, nup, use_ndn, ndn, use_n, n = [int(v) for v in sector]
-    sec = qk.Sector(sz2=sz2 if use_sz else None, n=n if use_n else None,
-                    nup=nup if use_nup else None, ndn=ndn if use_ndn else None)
-    cls = {0: (qk.SpinHalfBasis, qk.SpinHalfSite), 1: (qk.FermionBasis, qk.FermionSite),
-           2: (qk.HubbardBasis, qk.HubbardSite), 3: (qk.TJBasis, qk.TJSite)}[int(model)]
-    basis = qk.Basis.__new__(cls[0])
-    qk.Basis.__init__(basis, int(nsites), sec)
-    site = cls[1]()
-    ops = qk.OpSum()
-    for c, facs in terms:
-        args = []
-        for o, s in facs:
-            args += [o, s]
-        ops.add_term(c, *args)
-    return basis, site, ops
+from models import make_model  # noqa: E402,F401  (re-exported for the tests)
 

@@ -82,3 +82,22 @@ def xyz_field_terms(L, pbc, hx=0.3, hy=0.2, cplx=0.1):
     terms.append((complex(0.2, -0.05), [("Sp", 0), ("Sz", 1), ("Sm", 2)]))
     terms.append((complex(0.2, 0.05), [("Sm", 0), ("Sz", 1), ("Sp", 2)]))
     return terms
+
+
+def make_model(qk, model, nsites, sector, terms):
+    """Basis, site and OpSum objects of the GPU library for a model tuple."""
+    use_sz, sz2, use_nup, nup, use_ndn, ndn, use_n, n = [int(v) for v in sector]
+    sec = qk.Sector(sz2=sz2 if use_sz else None, n=n if use_n else None,
+                    nup=nup if use_nup else None, ndn=ndn if use_ndn else None)
+    cls = {0: (qk.SpinHalfBasis, qk.SpinHalfSite), 1: (qk.FermionBasis, qk.FermionSite),
+           2: (qk.HubbardBasis, qk.HubbardSite), 3: (qk.TJBasis, qk.TJSite)}[int(model)]
+    basis = qk.Basis.__new__(cls[0])
+    qk.Basis.__init__(basis, int(nsites), sec)
+    site = cls[1]()
+    ops = qk.OpSum()
+    for c, facs in terms:
+        args = []
+        for o, s in facs:
+            args += [o, s]
+        ops.add_term(c, *args)
+    return basis, site, ops
