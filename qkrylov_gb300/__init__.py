@@ -194,6 +194,7 @@ class Sector(_Handle):
     _destroy = "qkrylov_sector_destroy"
 
     def __init__(self, sz2=None, nup=None, ndn=None, n=None, nb=None):
+        self._q = {k: v for k, v in (("sz2", sz2), ("nup", nup), ("ndn", ndn), ("n", n), ("nb", nb)) if v is not None}
         self._h = lib().qkrylov_sector_create()
         if sz2 is not None:
             _check(lib().qkrylov_sector_set_sz(self._h, int(sz2)))
@@ -208,10 +209,18 @@ class Sector(_Handle):
         if nb is not None:
             _check(lib().qkrylov_sector_set_nb(self._h, int(nb)))
 
+    def describe(self):
+        """The quantum numbers set on this sector (e.g. {"sz2": 0})."""
+        return dict(self._q)
+
 
 class Basis(_Handle):
     _destroy = "qkrylov_basis_destroy"
     _create = None
+
+    @property
+    def sector(self):
+        return self._sector
 
     def __init__(self, N, sector=None):
         self._sector = sector
@@ -738,3 +747,6 @@ OpSum.__iadd__ = _opsum_iadd
 
 for _name in ("Sz", "Sp", "Sm", "Sx", "Sy", "CdagUp", "CUp", "CdagDn", "CDn", "Nup", "Ndn", "Nupdn", "N", "C", "Cdag", "Id"):
     globals()[_name] = (lambda nm: (lambda i: LocalOp(nm, i)))(_name)
+
+
+from . import io  # noqa: E402  (eigenvector / tridiagonal files)
