@@ -496,9 +496,9 @@ int qkrylov_lanczos_ground_state_f64(qkrylov_hamiltonian_h h, int maxiter, doubl
         o.tol = tol;
         o.want_vec = ev != nullptr;
         o.v0_ref = reinterpret_cast<const cd*>(v0);
+        o.evec_out = reinterpret_cast<cd*>(ev);
         const auto res = qkg::lanczos_f64(*h->ptr, o);
         fill_result(r, res);
-        if (ev) std::memcpy(ev, res.evec.data(), res.evec.size() * sizeof(cd));
     });
 }
 int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, double tol, const double* v0,
@@ -511,9 +511,9 @@ int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, dou
         o.tol = tol;
         o.want_vec = ev != nullptr;
         o.v0_ref = reinterpret_cast<const cd*>(v0);
+        o.evec_out = reinterpret_cast<cd*>(ev);
         const auto res = qkg::lanczos_mixed(*h->ptr, o);
         fill_result(r, res);
-        if (ev) std::memcpy(ev, res.evec.data(), res.evec.size() * sizeof(cd));
     });
 }
 int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed, const double* v0,
@@ -528,9 +528,9 @@ int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t s
         o.v0_ref = reinterpret_cast<const cd*>(v0);
         o.seed = seed;
         o.want_vec = ev != nullptr;
+        o.evec_out = reinterpret_cast<cd*>(ev);
         const auto res = mixed ? qkg::lanczos_mixed(*h->ptr, o) : qkg::lanczos_f64(*h->ptr, o);
         fill_result(r, res);
-        if (ev) std::memcpy(ev, res.evec.data(), res.evec.size() * sizeof(cd));
     });
 }
 

@@ -245,13 +245,23 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     if (o.device_start) {
         philox_normal_f32(o.seed, 0, v0, n, st);
     } else {
-        std::vector<cd> h(n);
-        if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
-        else ref_uniform_complex(1234, n, h.data(), o.f32_stream);
-        DBuf d64(n * sizeof(double2)), t64(n * sizeof(double2));
-        QKG_CUDA(cudaMemcpyAsync(t64.p, h.data(), n * sizeof(double2), cudaMemcpyHostToDevice, st));
-        H.to_internal_f64(t64.as<double2>(), d64.as<double2>(), st);
-        f64_to_f32(d64.as<double2>(), v0, n, st);
+        // the caller's vector is copied straight from its buffer (pinned memory takes the DMA path)
+        std::vector<cd> h;
+        const cd* src = o.v0_ref;
+        if (!src) {
+            h.resize(n);
+            ref_uniform_complex(1234, n, h.data(), o.f32_stream);
+            src = h.data();
+        }
+        DBuf t64(n * sizeof(double2)), d64;
+        QKG_CUDA(cudaMemcpyAsync(t64.p, src, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+        const double2* in = t64.as<double2>();
+        if (H.permuted()) {
+            d64.alloc(n * sizeof(double2));
+            H.to_internal_f64(t64.as<double2>(), d64.as<double2>(), st);
+            in = d64.as<double2>();
+        }
+        f64_to_f32(in, v0, n, st);
         QKG_CUDA(cudaStreamSynchronize(st));
     }
     const double nr0 = std::sqrt(nrm2sq_f32(v0, n, ws, st));
@@ -429,14 +439,19 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     out.energy = E;
     out.t_refine = secs(t1, clk::now());
     if (o.want_vec) {
-        out.evec.resize(n);
-        DBuf t2(n * sizeof(double2));
+        cd* dst = o.evec_out;
+        if (!dst) {
+            out.evec.resize(n);
+            dst = out.evec.data();
+        }
+        DBuf t2;
         const double2* src = r64.as<double2>();
         if (H.permuted()) {
+            t2.alloc(n * sizeof(double2));
             H.to_reference_f64(r64.as<double2>(), t2.as<double2>(), st);
             src = t2.as<double2>();
         }
-        QKG_CUDA(cudaMemcpyAsync(out.evec.data(), src, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        QKG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
         QKG_CUDA(cudaStreamSynchronize(st));
     }
     return out;

@@ -282,10 +282,15 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
     if (o.device_start) {
         philox_normal_f64(o.seed, 0, v, n, st);
     } else {
-        std::vector<cd> h(n);
-        if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
-        else ref_uniform_complex(1234, n, h.data(), o.f32_stream);  // src/solvers/lanczos.cpp:115-120
-        upload_ref_f64(H, h.data(), v, tmp);
+        std::vector<cd> h;
+        const cd* src = o.v0_ref;
+        if (!src) {
+            h.resize(n);
+            ref_uniform_complex(1234, n, h.data(), o.f32_stream);  // src/solvers/lanczos.cpp:115-120
+            src = h.data();
+        }
+        upload_ref_f64(H, src, v, tmp);
+        QKG_CUDA(cudaStreamSynchronize(st));
     }
     const double nr0 = std::sqrt(nrm2sq_f64(v, n, ws, st));
     if (nr0 != 0.0) scal_f64(1.0 / nr0, v, n, st);
@@ -341,8 +346,12 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
         mcombine_f64(V.dev(), (int)s.size(), cc.data(), ritz.as<double2>(), n, ws, st);
         const double nr = std::sqrt(nrm2sq_f64(ritz.as<double2>(), n, ws, st));
         if (nr != 0.0) scal_f64(1.0 / nr, ritz.as<double2>(), n, st);
-        out.evec.resize(n);
-        download_ref_f64(H, ritz.as<double2>(), out.evec.data(), tmp);
+        cd* dst = o.evec_out;
+        if (!dst) {
+            out.evec.resize(n);
+            dst = out.evec.data();
+        }
+        download_ref_f64(H, ritz.as<double2>(), dst, tmp);
     }
     return out;
 }
@@ -368,12 +377,17 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
     if (o.device_start) {
         philox_normal_f32(o.seed, 0, v, n, st);
     } else {
-        std::vector<cd> h(n);
-        if (o.v0_ref) std::copy(o.v0_ref, o.v0_ref + n, h.begin());
-        else ref_uniform_complex(1234, n, h.data());
+        std::vector<cd> h;
+        const cd* src = o.v0_ref;
+        if (!src) {
+            h.resize(n);
+            ref_uniform_complex(1234, n, h.data());
+            src = h.data();
+        }
         DBuf d64(n * sizeof(double2));
-        upload_ref_f64(H, h.data(), d64.as<double2>(), tmp);
+        upload_ref_f64(H, src, d64.as<double2>(), tmp);
         f64_to_f32(d64.as<double2>(), v, n, st);
+        QKG_CUDA(cudaStreamSynchronize(st));
     }
     const double nr0 = std::sqrt(nrm2sq_f32(v, n, ws, st));
     if (nr0 != 0.0) scal_f32(1.0 / nr0, v, n, st);
@@ -466,8 +480,12 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
     out.energy = E;
     out.t_refine = secs(t1, clk::now());
     if (o.want_vec) {
-        out.evec.resize(n);
-        download_ref_f64(H, r64.as<double2>(), out.evec.data(), tmp);
+        cd* dst = o.evec_out;
+        if (!dst) {
+            out.evec.resize(n);
+            dst = out.evec.data();
+        }
+        download_ref_f64(H, r64.as<double2>(), dst, tmp);
     }
     return out;
 }

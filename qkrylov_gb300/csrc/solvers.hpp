@@ -68,6 +68,7 @@ struct LanczosOpts {
     bool device_start = false;   // seeded Philox Gaussian start (performance runs)
     uint64_t seed = 0;
     bool f32_stream = false;     // draw the start vector as the reference's FP32 engine does
+    cd* evec_out = nullptr;      // with want_vec: the Ritz vector goes here (reference order) instead of LanczosOut::evec
 };
 struct LanczosOut {
     double energy = 0.0;       // reported energy (refined for the mixed form)
