@@ -33,6 +33,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 
 namespace qkg {
 using namespace fastk;
@@ -631,7 +633,28 @@ BlockTridiag run_block(const std::vector<Hamiltonian*>& hs, const BlockOpts& o, 
             }
         }
     }
-    const int vpl = o.vpl > 0 ? o.vpl : E.autotune(out.tune_ms);
+    // tile shape: autotuned once per batch of Hamiltonians, vector width and precision
+    int vpl = o.vpl;
+    if (vpl <= 0) {
+        static std::mutex mu;
+        static std::map<std::vector<uintptr_t>, std::pair<int, std::vector<double>>> cache;
+        std::vector<uintptr_t> key;
+        for (auto* h : hs) {
+            key.push_back(reinterpret_cast<uintptr_t>(h));
+            key.push_back((uintptr_t)h->dim());
+        }
+        key.push_back((uintptr_t)Rp);
+        key.push_back((uintptr_t)sizeof(T));
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            vpl = E.autotune(out.tune_ms);
+            cache[key] = {vpl, out.tune_ms};
+        } else {
+            vpl = it->second.first;
+            out.tune_ms = it->second.second;
+        }
+    }
     QKG_REQUIRE(Rp % vpl == 0 && Rp / vpl <= 32, "vectors per lane must divide the padded block width");
     out.vpl = vpl;
     // the autotuner wrote into buffer 1: clear it again (it is u_{-1} at step 0)

@@ -584,6 +584,7 @@ void ftlm_observables(const std::vector<FTLMTri>& tri, const double* betas, int 
     double emin = std::numeric_limits<double>::infinity();
     for (const auto& t : tri) for (double e : t.evals) emin = std::min(emin, e);
     const int R = (int)tri.size();
+#pragma omp parallel for schedule(dynamic, 1)
     for (int k = 0; k < nb; ++k) {
         const double beta = betas[k];
         const double sh = shifted ? emin : 0.0;
