@@ -225,13 +225,16 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     // all nmax + 1 Krylov vectors (FP32) up front: the graph addresses them through vtab
     size_t fr = 0, tot = 0;
     QKG_CUDA(cudaMemGetInfo(&fr, &tot));
-    const size_t need = (size_t)(nmax + 1) * n * sizeof(float2);
+    // vectors start on 256-byte boundaries (a warp's 32 consecutive rows then
+    // cover whole 128-byte lines)
+    const uint64_t stride = (n + 31) / 32 * 32;
+    const size_t need = (size_t)(nmax + 1) * stride * sizeof(float2);
     if (need + (512ull << 20) > fr)
         throw Error(CUDA_ERR, "out of device memory for " + std::to_string(nmax + 1) + " Krylov vectors");
     // one allocation for all vectors (a cudaMalloc per vector costs more than a step)
-    DBuf V((size_t)(nmax + 1) * n * sizeof(float2));
+    DBuf V(need);
     std::vector<void*> vptr;
-    for (int i = 0; i <= nmax; ++i) vptr.push_back(V.as<float2>() + (size_t)i * n);
+    for (int i = 0; i <= nmax; ++i) vptr.push_back(V.as<float2>() + (size_t)i * stride);
     DBuf vtab((nmax + 1) * sizeof(void*));
     QKG_CUDA(cudaMemcpy(vtab.p, vptr.data(), vptr.size() * sizeof(void*), cudaMemcpyHostToDevice));
     DBuf state(sizeof(LzState)), alpha((nmax + 2) * 8), beta((nmax + 2) * 8), sig((nmax + 2) * 8);
