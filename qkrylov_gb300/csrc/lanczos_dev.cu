@@ -65,18 +65,36 @@ __device__ __forceinline__ double2 bsum2(double x, double y) {
     return v;
 }
 
+// alpha from the SpMV's per-CTA partials: kAlphaBlocks blocks sum fixed
+// slices, the last block to finish (arrival counter) adds their sums in block
+// order and does the step's bookkeeping; the result does not depend on which
+// block finishes last.
+constexpr int kAlphaBlocks = 64;
 __global__ void lz_alpha_kernel(const double2* __restrict__ apart, int nparts, LzState* st, double* alpha,
-                                const double* beta, const double* sig, double* alpha_host) {
+                                const double* beta, const double* sig, double* alpha_host, double* part2,
+                                unsigned int* arrived) {
     double s = 0.0;
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += apart[i].x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nparts; i += gridDim.x * blockDim.x) s += apart[i].x;
     const double2 t = bsum2(s, 0.0);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        part2[blockIdx.x] = t.x;
+        __threadfence();
+        last = atomicAdd(arrived, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double v = threadIdx.x < gridDim.x ? *(volatile double*)(part2 + threadIdx.x) : 0.0;
+    const double2 u = bsum2(v, 0.0);
     if (threadIdx.x == 0) {
         const int k = st->k;
-        const double a = sig[k] * t.x;
+        const double a = sig[k] * u.x;
         alpha[k] = a;
         alpha_host[k] = a;
         st->a = a * sig[k];
         st->b = k > 0 ? beta[k - 1] * sig[k - 1] : 0.0;
+        *arrived = 0u;  // ready for the next step
     }
 }
 
@@ -241,6 +259,8 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     DBuf apart(std::max<size_t>(1, H.lanczos_parts()) * sizeof(double2)), bpart(kUpdGrid * sizeof(double2)),
         ppart(kUpdGrid * sizeof(double2));
     Mapped ah(nmax + 2), bh(nmax + 2);
+    DBuf part2(kAlphaBlocks * sizeof(double)), arrived(sizeof(unsigned int));
+    QKG_CUDA(cudaMemsetAsync(arrived.p, 0, sizeof(unsigned int), st));
     Workspace ws(std::max<size_t>(1 << 16, (size_t)1216 * (size_t)(nmax + 2)));
     DBuf tmp;
 
@@ -288,8 +308,9 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
         if (timer) timer->start();
         H.apply_lanczos_f32(hooks, st);
         if (timer) timer->stop();
-        lz_alpha_kernel<<<1, kT, 0, st>>>(apart.as<double2>(), nparts, state.as<LzState>(), alpha.as<double>(),
-                                          beta.as<double>(), sig.as<double>(), ah.d);
+        lz_alpha_kernel<<<kAlphaBlocks, kT, 0, st>>>(apart.as<double2>(), nparts, state.as<LzState>(),
+                                                     alpha.as<double>(), beta.as<double>(), sig.as<double>(), ah.d,
+                                                     part2.as<double>(), arrived.as<unsigned int>());
         QKG_LAUNCHED();
         if (!so) {
             lz_update_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
