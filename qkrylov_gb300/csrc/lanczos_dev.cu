@@ -98,68 +98,67 @@ __global__ void lz_alpha_kernel(const double2* __restrict__ apart, int nparts, L
     }
 }
 
-__global__ void lz_update_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st, uint64_t n,
-                                 double2* __restrict__ bpart) {
-    const int k = st->k;
-    float2* __restrict__ w = static_cast<float2*>(vtab[k + 1]);
-    const float2* __restrict__ v = static_cast<const float2*>(vtab[k]);
-    const float2* __restrict__ vp = k > 0 ? static_cast<const float2*>(vtab[k - 1]) : nullptr;
-    const float a = (float)st->a, b = (float)st->b;
-    float hi = 0.f, lo = 0.f;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        float2 x = w[i];
-        const float2 c = v[i];
-        x.x = fmaf(-a, c.x, x.x);
-        x.y = fmaf(-a, c.y, x.y);
-        if (vp) {
-            const float2 d = vp[i];
-            x.x = fmaf(-b, d.x, x.x);
-            x.y = fmaf(-b, d.y, x.y);
-        }
-        w[i] = x;
-        ff_acc(hi, lo, x.x, x.x);
-        ff_acc(hi, lo, x.y, x.y);
+// One element of the update w -= a v + b v_prev with its ||w||^2 (and, with
+// psi, <psi, w>) contributions.
+struct UpdAcc {
+    float hi = 0.f, lo = 0.f, rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+};
+template <bool PROJ>
+__device__ __forceinline__ float2 upd_elem(float2 x, float2 c, float2 d, float2 p, float a, float b, bool has_prev,
+                                           UpdAcc& s) {
+    x.x = fmaf(-a, c.x, x.x);
+    x.y = fmaf(-a, c.y, x.y);
+    if (has_prev) {
+        x.x = fmaf(-b, d.x, x.x);
+        x.y = fmaf(-b, d.y, x.y);
     }
-    const double2 s = bsum2((double)hi + (double)lo, 0.0);
-    if (threadIdx.x == 0) bpart[blockIdx.x] = s;
+    ff_acc(s.hi, s.lo, x.x, x.x);
+    ff_acc(s.hi, s.lo, x.y, x.y);
+    if (PROJ) {
+        ff_acc(s.rh, s.rl, p.x, x.x);
+        ff_acc(s.rh, s.rl, p.y, x.y);
+        ff_acc(s.ih, s.il, p.x, x.y);
+        ff_acc(s.ih, s.il, -p.y, x.x);
+    }
+    return x;
 }
 
-// The update of lz_update_kernel fused with the partials of <psi, W>
-// (selective reorthogonalisation): one pass over W, v, v_prev and psi.
-__global__ void lz_update_proj_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st, uint64_t n,
-                                      const float2* __restrict__ psi, double2* __restrict__ bpart,
-                                      double2* __restrict__ ppart) {
+// w -= a v + b v_prev in place, ||w||^2 partials (and <psi, w> partials with
+// PROJ, for selective reorthogonalisation): two elements per thread and
+// iteration with 16-byte accesses (the Krylov vectors are 256-byte aligned).
+template <bool PROJ>
+__global__ void lz_update_t(void* const* __restrict__ vtab, const LzState* __restrict__ st, uint64_t n,
+                            const float2* __restrict__ psi, double2* __restrict__ bpart,
+                            double2* __restrict__ ppart) {
     const int k = st->k;
     float2* __restrict__ w = static_cast<float2*>(vtab[k + 1]);
     const float2* __restrict__ v = static_cast<const float2*>(vtab[k]);
-    const float2* __restrict__ vp = k > 0 ? static_cast<const float2*>(vtab[k - 1]) : nullptr;
+    const float2* __restrict__ vp = k > 0 ? static_cast<const float2*>(vtab[k - 1]) : v;
+    const bool has_prev = k > 0;
     const float a = (float)st->a, b = (float)st->b;
-    float hi = 0.f, lo = 0.f, rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        float2 x = w[i];
-        const float2 c = v[i];
-        x.x = fmaf(-a, c.x, x.x);
-        x.y = fmaf(-a, c.y, x.y);
-        if (vp) {
-            const float2 d = vp[i];
-            x.x = fmaf(-b, d.x, x.x);
-            x.y = fmaf(-b, d.y, x.y);
-        }
-        w[i] = x;
-        ff_acc(hi, lo, x.x, x.x);
-        ff_acc(hi, lo, x.y, x.y);
-        const float2 p = psi[i];
-        ff_acc(rh, rl, p.x, x.x);
-        ff_acc(rh, rl, p.y, x.y);
-        ff_acc(ih, il, p.x, x.y);
-        ff_acc(ih, il, -p.y, x.x);
+    UpdAcc s;
+    const uint64_t n2 = n / 2, step = (uint64_t)gridDim.x * blockDim.x;
+    const float2 zero = make_float2(0.f, 0.f);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n2; i += step) {
+        const float4 x4 = reinterpret_cast<const float4*>(w)[i];
+        const float4 c4 = reinterpret_cast<const float4*>(v)[i];
+        const float4 d4 = reinterpret_cast<const float4*>(vp)[i];
+        float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (PROJ) p4 = reinterpret_cast<const float4*>(psi)[i];
+        const float2 y0 = upd_elem<PROJ>(make_float2(x4.x, x4.y), make_float2(c4.x, c4.y), make_float2(d4.x, d4.y),
+                                         make_float2(p4.x, p4.y), a, b, has_prev, s);
+        const float2 y1 = upd_elem<PROJ>(make_float2(x4.z, x4.w), make_float2(c4.z, c4.w), make_float2(d4.z, d4.w),
+                                         make_float2(p4.z, p4.w), a, b, has_prev, s);
+        reinterpret_cast<float4*>(w)[i] = make_float4(y0.x, y0.y, y1.x, y1.y);
     }
-    const double2 s = bsum2((double)hi + (double)lo, 0.0);
-    const double2 q = bsum2((double)rh + (double)rl, (double)ih + (double)il);
-    if (threadIdx.x == 0) {
-        bpart[blockIdx.x] = s;
-        ppart[blockIdx.x] = q;
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        w[n - 1] = upd_elem<PROJ>(w[n - 1], v[n - 1], vp[n - 1], PROJ ? psi[n - 1] : zero, a, b, has_prev, s);
+    const double2 t = bsum2((double)s.hi + (double)s.lo, 0.0);
+    if (PROJ) {
+        const double2 q = bsum2((double)s.rh + (double)s.rl, (double)s.ih + (double)s.il);
+        if (threadIdx.x == 0) ppart[blockIdx.x] = q;
     }
+    if (threadIdx.x == 0) bpart[blockIdx.x] = t;
 }
 
 // c = <psi, W>; the correction is applied only when |c| exceeds orth_tol ||W||
@@ -313,12 +312,12 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
                                                      part2.as<double>(), arrived.as<unsigned int>());
         QKG_LAUNCHED();
         if (!so) {
-            lz_update_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
-                                                      bpart.as<double2>());
+            lz_update_t<false><<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
+                                                        nullptr, bpart.as<double2>(), nullptr);
             QKG_LAUNCHED();
         } else {
-            lz_update_proj_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
-                                                           psi.as<float2>(), bpart.as<double2>(), ppart.as<double2>());
+            lz_update_t<true><<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
+                                                       psi.as<float2>(), bpart.as<double2>(), ppart.as<double2>());
             QKG_LAUNCHED();
             lz_proj_finish_kernel<<<1, kT, 0, st>>>(ppart.as<double2>(), bpart.as<double2>(), kUpdGrid,
                                                     state.as<LzState>(), kOrthTol);
