@@ -393,7 +393,7 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* no, int* ni, int* nm,
 }
 
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use) {
-    if (!h || !h->ptr || generic < 0 || generic > 5) return QKRYLOV_ERROR_INVALID_ARG;
+    if (!h || !h->ptr || generic < 0 || generic > 6) return QKRYLOV_ERROR_INVALID_ARG;
     h->ptr->set_kernel_mode(generic);
     if (fast_in_use) *fast_in_use = h->ptr->fast() ? 1 : 0;
     return QKRYLOV_SUCCESS;
@@ -404,7 +404,7 @@ int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, 
     const auto& H = *h->ptr;
     *variant = H.fast() ? (int)H.variant(fp32 ? 8 : 16) : -1;
     if (ms)
-        for (int v = 0; v < 4; ++v) ms[v] = H.tuned_ms(fp32 ? 0 : 1, v);
+        for (int v = 0; v < qkg::kFastVariants; ++v) ms[v] = H.tuned_ms(fp32 ? 0 : 1, v);
     return QKRYLOV_SUCCESS;
 }
 

@@ -429,11 +429,16 @@ static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread
 #ifndef QKG_ELL_PREFETCH
 #define QKG_ELL_PREFETCH 1
 #endif
-template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (STAGE ? QKG_ROWS_MINB - 1 : QKG_ROWS_MINB) : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
+#ifndef QKG_ALT_RT
+#define QKG_ALT_RT 2
+#endif
+#ifndef QKG_ROWS2_MINB
+#define QKG_ROWS2_MINB (QKG_ALT_RT == 2 ? 6 : QKG_ALT_RT == 8 ? 3 : 5)
+#endif
+template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE, int RT = kRowsPerThread>
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (RT != kRowsPerThread ? QKG_ROWS2_MINB : (STAGE ? QKG_ROWS_MINB - 1 : QKG_ROWS_MINB)) : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
                                                            typename V2<T>::t* __restrict__ y_in) {
     using T2 = typename V2<T>::t;
-    constexpr int RT = kRowsPerThread;
     extern __shared__ __align__(16) unsigned char rows_smem[];
     T2* xs = reinterpret_cast<T2*>(rows_smem);  // STAGE: the outer block's slice of x
     const T2* __restrict__ x = x_in;
@@ -502,7 +507,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (STAGE ? QKG_ROWS_MIN
 
     A dot_hi = 0, dot_lo = 0;
     // passes of kChunk rows (one pass unless a whole outer block is staged)
-    for (uint32_t pass = 0; pass < (STAGE ? it.count : 1u); pass += kChunk) {
+    for (uint32_t pass = 0; pass < (STAGE ? it.count : 1u); pass += RT * kBlock) {
     uint32_t s[RT], e0[RT], e1[RT];
     A ar_[RT], ai_[RT];
     bool live[RT];
@@ -948,6 +953,10 @@ void Hamiltonian::build_fast() {
         auto items = B.work_items(kChunk);
         set_groups(items);
         upload_vec(items_, items);
+        auto items2 = B.work_items(QKG_ALT_RT * kBlock);
+        set_groups(items2);
+        n_items_r2_ = items2.size();
+        upload_vec(items_r2_, items2);
     }
     u_ar_ = amp0.real();
     u_ai_ = amp0.imag();
@@ -997,9 +1006,9 @@ void Hamiltonian::autotune() {
         QKG_CUDA(cudaEventCreate(&a));
         QKG_CUDA(cudaEventCreate(&b));
         double best = 0.0;
-        for (int v = 0; v < 4; ++v) {
+        for (int v = 0; v < kFastVariants; ++v) {
             if ((v == FV_STAGED || v == FV_ROWS4_STAGED) && !(max_block_ * e <= kStageLimit)) continue;
-            mode_ = v == FV_ROW ? 2 : v == FV_STAGED ? 3 : v == FV_ROWS4 ? 4 : 5;
+            mode_ = 2 + v;  // modes 2..6 select variants 0..4
             auto run = [&] {
                 if (prec) apply_f64(x.as<double2>(), y.as<double2>(), stream_);
                 else apply_f32(x.as<float2>(), y.as<float2>(), stream_);
@@ -1130,6 +1139,20 @@ static void launch_fast(const FastParams<A>& p, size_t n_items, bool real, bool 
     const unsigned g = (unsigned)n_items;
     const int key = (var == FV_STAGED ? 8 : 0) | (real ? 4 : 0) | (unif ? 2 : 0) | (outer_has_j ? 1 : 0);
     const size_t sm = stage_smem;
+    if (var == FV_ROWS2) {
+        switch (key & 7) {
+            case 0: spmv_rows_kernel<T, A, false, false, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 1: spmv_rows_kernel<T, A, false, false, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 2: spmv_rows_kernel<T, A, false, true, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 3: spmv_rows_kernel<T, A, false, true, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 4: spmv_rows_kernel<T, A, true, false, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 5: spmv_rows_kernel<T, A, true, false, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 6: spmv_rows_kernel<T, A, true, true, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            default: spmv_rows_kernel<T, A, true, true, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+        }
+        QKG_LAUNCHED();
+        return;
+    }
     if (var == FV_ROWS4 || var == FV_ROWS4_STAGED) {
         const bool st = var == FV_ROWS4_STAGED;
         switch ((st ? 8 : 0) | (key & 7)) {
@@ -1313,9 +1336,9 @@ void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const 
         const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
         FastParams<double> p;
         fast_params(p);
-        if (st) p.items = items_blk_.as<WorkItem>();
-        launch_fast<double, double>(p, st ? n_items_blk_ : n_items_, all_real_, unif_, x, y, s, v,
-                                    st ? max_block_ * 16 : 0);
+        size_t ni = 0;
+        p.items = items_of(v, &ni);
+        launch_fast<double, double>(p, ni, all_real_, unif_, x, y, s, v, st ? max_block_ * 16 : 0);
         return;
     }
     const DBuf& full = dfull64_;
@@ -1331,19 +1354,33 @@ void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) cons
     const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
     FastParams<float> p;
     fast_params(p);
-    if (st) p.items = items_blk_.as<WorkItem>();
+    size_t ni = 0;
+    p.items = items_of(v, &ni);
     p.vtab = lz.vtab;
     p.kstep = lz.kstep;
     p.sig = lz.sig;
     p.apart = lz.apart;
-    launch_fast<float, float>(p, st ? n_items_blk_ : n_items_, all_real_, unif_, nullptr, nullptr, s, v,
-                              st ? max_block_ * 8 : 0);
+    launch_fast<float, float>(p, ni, all_real_, unif_, nullptr, nullptr, s, v, st ? max_block_ * 8 : 0);
 }
 
 size_t Hamiltonian::lanczos_parts() const {
     if (!fast()) return n_items_;
-    const FastVariant v = variant(8);
-    return (v == FV_STAGED || v == FV_ROWS4_STAGED) ? n_items_blk_ : n_items_;
+    size_t ni = 0;
+    items_of(variant(8), &ni);
+    return ni;
+}
+
+const WorkItem* Hamiltonian::items_of(FastVariant v, size_t* n) const {
+    if (v == FV_STAGED || v == FV_ROWS4_STAGED) {
+        *n = n_items_blk_;
+        return items_blk_.as<WorkItem>();
+    }
+    if (v == FV_ROWS2) {
+        *n = n_items_r2_;
+        return items_r2_.as<WorkItem>();
+    }
+    *n = n_items_;
+    return items_.as<WorkItem>();
 }
 
 void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
@@ -1352,9 +1389,9 @@ void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
         const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
         FastParams<float> p;
         fast_params(p);
-        if (st) p.items = items_blk_.as<WorkItem>();
-        launch_fast<float, float>(p, st ? n_items_blk_ : n_items_, all_real_, unif_, x, y, s, v,
-                                  st ? max_block_ * 8 : 0);
+        size_t ni = 0;
+        p.items = items_of(v, &ni);
+        launch_fast<float, float>(p, ni, all_real_, unif_, x, y, s, v, st ? max_block_ * 8 : 0);
         return;
     }
     if (wide_)

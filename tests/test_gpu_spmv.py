@@ -83,8 +83,8 @@ def test_entries_bit_exact(qk, name):
     np.testing.assert_allclose(vals, g["csr_vals"], rtol=0, atol=1e-15)
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5],
-                         ids=["auto", "generic", "fast", "fast-staged", "fast-rows4", "fast-rows4-staged"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6],
+                         ids=["auto", "generic", "fast", "fast-staged", "fast-rows4", "fast-rows4-staged", "fast-rows2"])
 @pytest.mark.parametrize("name", golden_names())
 def test_apply_and_diagonal(qk, name, mode):
     g = load_golden(name)
@@ -126,7 +126,7 @@ def test_apply_against_oracle(qk, oracle, model, N, sector, terms):
     rng = np.random.default_rng(7)
     x = rng.normal(size=o.dim) + 1j * rng.normal(size=o.dim)
     yo = o.apply(x)
-    for mode in (0, 1, 2, 3, 4, 5):
+    for mode in (0, 1, 2, 3, 4, 5, 6):
         H.select_kernel(mode=mode)
         y = H.apply(x)
         assert np.abs(y - yo).max() <= RTOL64 * np.abs(yo).max()
