@@ -286,7 +286,7 @@ def main():
     tr = profile_traffic()
     variant, _ = H.tuning(fp32=True)
     kname = {"rows4": "spmv_rows_kernel<float>", "rows4_staged": "spmv_rows_kernel<float, staged>",
-             "rows2": "spmv_rows_kernel<float, 2 rows>",
+             "rows4_wide": "spmv_rows_kernel<float, 4 CTAs/SM>",
              "row": "spmv_fast_kernel<float>",
              "staged": "spmv_fast_kernel<float, staged>"}.get(variant, "spmv_kernel<float>")
     out["roofline"] = {"kernel": kname + " (FP32 SpMV)", "bound": "hbm", "achieved": achieved,

@@ -283,13 +283,14 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* n_outer, int* n_inner
  * the generic kernel; 2 the fast kernel with one row per thread; 3 the fast
  * kernel with shared-memory staging of each outer block's slice of x (when a
  * block fits); 4 the fast kernel with four rows per thread; 5 four rows per
- * thread with the block staged (when it fits); 6 two rows per thread.
+ * thread with the block staged (when it fits); 6 four rows per thread with a
+ * larger register budget.
  * *fast_in_use (optional) reports whether the fast kernel applies. */
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use);
 
 /* The fast-kernel variant mode 0 uses for FP32 (fp32 != 0) or FP64 vectors
  * (*variant: 0 one row per thread, 1 staged, 2 four rows per thread, 3 four
- * rows per thread staged, 4 two rows per thread; -1 when the generic kernel
+ * rows per thread staged, 4 four rows per thread wide; -1 when the generic kernel
  * applies) and the autotuner's mean launch times per variant
  * (ms_per_variant[5], 0 = not measured; sectors below 2^20 rows are not
  * timed). */

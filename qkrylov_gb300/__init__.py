@@ -381,7 +381,8 @@ class MatrixFreeHamiltonian(_Handle):
         """Force the generic SpMV kernel (True) or allow the fast one (False).
         mode picks a kernel directly: 0 autotuned, 1 generic, 2 fast with one
         row per thread, 3 fast with shared-memory staging, 4 fast with four
-        rows per thread, 5 four rows per thread staged, 6 two rows per thread.
+        rows per thread, 5 four rows per thread staged, 6 four rows per thread
+        with a larger register budget.
         Returns whether the fast kernel is in use."""
         m = int(mode) if mode is not None else int(bool(generic))
         f = _c.c_int()
@@ -394,7 +395,7 @@ class MatrixFreeHamiltonian(_Handle):
         v = _c.c_int()
         ms = (_c.c_double * 5)()
         _check(lib().qkrylov_hamiltonian_tuning(self._h, int(bool(fp32)), _c.byref(v), ms))
-        names = ["row", "staged", "rows4", "rows4_staged", "rows2"]
+        names = ["row", "staged", "rows4", "rows4_staged", "rows4_wide"]
         return ("generic" if v.value < 0 else names[v.value]), {names[i]: ms[i] for i in range(5)}
 
     def benchmark_apply(self, fp32=True, reps=10):

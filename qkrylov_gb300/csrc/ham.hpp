@@ -31,8 +31,8 @@ enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
 
 // Fast SpMV kernel variants: one row per thread, the outer block's slice of x
 // staged in shared memory, four rows per thread, four rows per thread with the
-// block staged, two rows per thread.
-enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3, FV_ROWS2 = 4 };
+// block staged, four rows per thread with a larger register budget.
+enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3, FV_ROWS4_WIDE = 4 };
 constexpr int kFastVariants = 5;
 
 // Device-resident Lanczos step: the SpMV reads its vectors through a device
@@ -102,8 +102,8 @@ public:
     bool fast() const { return fast_ && !force_generic_; }
     // kernel mode: 0 automatic (autotuned), 1 generic kernel, 2 fast kernel
     // one row per thread, 3 fast kernel with shared-memory staging, 4 fast
-    // kernel four rows per thread, 5 four rows per thread with staging, 6 two
-    // rows per thread
+    // kernel four rows per thread, 5 four rows per thread with staging, 6 four
+    // rows per thread with the larger register budget
     void set_kernel_mode(int m) { mode_ = m; force_generic_ = (m == 1); }
     void force_generic(bool on) { set_kernel_mode(on ? 1 : 0); }
     // fast-kernel variant for vectors of elem_bytes per element
@@ -113,7 +113,7 @@ public:
         if (mode_ == 3) return can_stage ? FV_STAGED : FV_ROW;
         if (mode_ == 4) return FV_ROWS4;
         if (mode_ == 5) return can_stage ? FV_ROWS4_STAGED : FV_ROWS4;
-        if (mode_ == 6) return FV_ROWS2;
+        if (mode_ == 6) return FV_ROWS4_WIDE;
         const FastVariant v = pref_[elem_bytes == 16 ? 1 : 0];
         if (v == FV_STAGED && !can_stage) return FV_ROW;
         if (v == FV_ROWS4_STAGED && !can_stage) return FV_ROWS4;
@@ -153,8 +153,6 @@ private:
     FastVariant pref_[2] = {FV_ROWS4, FV_ROWS4};
     double tune_ms_[2][kFastVariants] = {};
     DBuf items_blk_;            // one work item per outer block (staged kernel)
-    DBuf items_r2_;             // work items of 512 rows (two rows per thread)
-    size_t n_items_r2_ = 0;
     size_t n_items_blk_ = 0, max_block_ = 0;
     double u_ar_ = 0.0, u_ai_ = 0.0;
     int rbits_ = 0;

@@ -429,14 +429,13 @@ static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread
 #ifndef QKG_ELL_PREFETCH
 #define QKG_ELL_PREFETCH 1
 #endif
-#ifndef QKG_ALT_RT
-#define QKG_ALT_RT 2
+#ifndef QKG_ROWS_MINB_WIDE
+#define QKG_ROWS_MINB_WIDE 4
 #endif
-#ifndef QKG_ROWS2_MINB
-#define QKG_ROWS2_MINB (QKG_ALT_RT == 2 ? 6 : QKG_ALT_RT == 8 ? 3 : 5)
-#endif
-template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE, int RT = kRowsPerThread>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (RT != kRowsPerThread ? QKG_ROWS2_MINB : (STAGE ? QKG_ROWS_MINB - 1 : QKG_ROWS_MINB)) : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
+// WIDE: a larger register budget (4 instead of 5 resident CTAs per SM), which
+// pays where straddling terms keep more state live.
+template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE, bool WIDE = false, int RT = kRowsPerThread>
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB_WIDE : (STAGE ? QKG_ROWS_MINB - 1 : QKG_ROWS_MINB)) : QKG_ROWS_MINB64) spmv_rows_kernel(const FastParams<A> p, const typename V2<T>::t* __restrict__ x_in,
                                                            typename V2<T>::t* __restrict__ y_in) {
     using T2 = typename V2<T>::t;
     extern __shared__ __align__(16) unsigned char rows_smem[];
@@ -949,14 +948,26 @@ void Hamiltonian::build_fast() {
             w.pad = class_gbase[m] + r_loc / 32;
         }
     };
+    // Launch order of the work items.  A straddling term that flips a high
+    // outer bit (the periodic bond of a chain) gathers from the block half a
+    // vector away, at scattered rows; ordering the items so that the two blocks
+    // of each such pair run side by side keeps those rows in L2.
+    int pair_bit = -1;
+    for (const HostTerm* h : mixed) {
+        const uint64_t xo = (h->X & ~inm) >> B.n_in;
+        if ((h->X & inm) && xo) pair_bit = std::max(pair_bit, 63 - __builtin_clzll(xo));
+    }
+    auto pair_order = [&](std::vector<WorkItem>& v) {
+        if (pair_bit < 0) return;
+        const uint32_t m = 1u << pair_bit;
+        auto key = [&](const WorkItem& w) { return ((uint64_t)(w.a & ~m) << 1) | ((w.a & m) ? 1u : 0u); };
+        std::stable_sort(v.begin(), v.end(), [&](const WorkItem& x, const WorkItem& y) { return key(x) < key(y); });
+    };
     {
         auto items = B.work_items(kChunk);
         set_groups(items);
+        pair_order(items);
         upload_vec(items_, items);
-        auto items2 = B.work_items(QKG_ALT_RT * kBlock);
-        set_groups(items2);
-        n_items_r2_ = items2.size();
-        upload_vec(items_r2_, items2);
     }
     u_ar_ = amp0.real();
     u_ai_ = amp0.imag();
@@ -982,6 +993,7 @@ void Hamiltonian::build_fast() {
     // one item per outer block for the staged kernel
     auto bitems = B.work_items(0xFFFFFFFFu);
     set_groups(bitems);
+    pair_order(bitems);
     max_block_ = 0;
     for (const auto& w : bitems) max_block_ = std::max<size_t>(max_block_, w.count);
     n_items_blk_ = bitems.size();
@@ -1139,16 +1151,16 @@ static void launch_fast(const FastParams<A>& p, size_t n_items, bool real, bool 
     const unsigned g = (unsigned)n_items;
     const int key = (var == FV_STAGED ? 8 : 0) | (real ? 4 : 0) | (unif ? 2 : 0) | (outer_has_j ? 1 : 0);
     const size_t sm = stage_smem;
-    if (var == FV_ROWS2) {
+    if (var == FV_ROWS4_WIDE) {
         switch (key & 7) {
-            case 0: spmv_rows_kernel<T, A, false, false, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 1: spmv_rows_kernel<T, A, false, false, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 2: spmv_rows_kernel<T, A, false, true, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 3: spmv_rows_kernel<T, A, false, true, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 4: spmv_rows_kernel<T, A, true, false, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 5: spmv_rows_kernel<T, A, true, false, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            case 6: spmv_rows_kernel<T, A, true, true, false, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
-            default: spmv_rows_kernel<T, A, true, true, true, false, QKG_ALT_RT><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 0: spmv_rows_kernel<T, A, false, false, false, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 1: spmv_rows_kernel<T, A, false, false, true, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 2: spmv_rows_kernel<T, A, false, true, false, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 3: spmv_rows_kernel<T, A, false, true, true, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 4: spmv_rows_kernel<T, A, true, false, false, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 5: spmv_rows_kernel<T, A, true, false, true, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            case 6: spmv_rows_kernel<T, A, true, true, false, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
+            default: spmv_rows_kernel<T, A, true, true, true, false, true><<<g, kBlock, 0, s>>>(p, x, y); break;
         }
         QKG_LAUNCHED();
         return;
@@ -1374,10 +1386,6 @@ const WorkItem* Hamiltonian::items_of(FastVariant v, size_t* n) const {
     if (v == FV_STAGED || v == FV_ROWS4_STAGED) {
         *n = n_items_blk_;
         return items_blk_.as<WorkItem>();
-    }
-    if (v == FV_ROWS2) {
-        *n = n_items_r2_;
-        return items_r2_.as<WorkItem>();
     }
     *n = n_items_;
     return items_.as<WorkItem>();

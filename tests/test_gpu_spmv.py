@@ -84,7 +84,7 @@ def test_entries_bit_exact(qk, name):
 
 
 @pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6],
-                         ids=["auto", "generic", "fast", "fast-staged", "fast-rows4", "fast-rows4-staged", "fast-rows2"])
+                         ids=["auto", "generic", "fast", "fast-staged", "fast-rows4", "fast-rows4-staged", "fast-rows4-wide"])
 @pytest.mark.parametrize("name", golden_names())
 def test_apply_and_diagonal(qk, name, mode):
     g = load_golden(name)
