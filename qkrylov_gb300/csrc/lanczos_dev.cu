@@ -330,6 +330,7 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
                                          sig.as<double>(), bh.d);
         QKG_LAUNCHED();
     };
+    int kernels_plain = 0, kernels_so = 0;  // kernels per step graph, counted at capture
     auto capture = [&](bool so) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
@@ -337,12 +338,13 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
         QKG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         enqueue_step(so, nullptr);
         QKG_CUDA(cudaStreamEndCapture(st, &g));
-        add_launches(-(int64_t)(launch_count() - c0));
+        const int64_t captured = (int64_t)(launch_count() - c0);
+        add_launches(-captured);
+        (so ? kernels_so : kernels_plain) = (int)captured;  // kernels per replay
         QKG_CUDA(cudaGraphInstantiate(&ge, g, 0));
         QKG_CUDA(cudaGraphDestroy(g));
         return ge;
     };
-    const int kernels_plain = 4, kernels_so = 6;
     cudaGraphExec_t g_plain = nullptr, g_so = nullptr;
     std::vector<cudaEvent_t> ev(kInFlight + 2);
     for (auto& e : ev) QKG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
