@@ -615,19 +615,33 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     }
 #endif
     for (int k = 0; k < p.n_mixed; ++k) {
-        const uint32_t C = mixed[k].C, V = mixed[k].V;
+        // the four rows' targets first (their rank lookups in flight together),
+        // then the gathers, then the sums
+        const KTerm<uint32_t, A> t = mixed[k];
+        uint32_t idx[RT];
+        bool ok[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q) {
-            if (!live[q] || (s[q] & C) != V) continue;
-            const KTerm<uint32_t, A> t = mixed[k];
+            ok[q] = live[q] && (s[q] & t.C) == t.V;
             const uint32_t s2 = s[q] ^ t.X;
-            if ((t.flags & 1u) && !in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2))
-                continue;
-            const uint32_t b2 = s2 & p.in_mask;
-            const uint32_t idx = __ldg(p.outer_off + (s2 >> p.n_in)) + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+            if (ok[q] && (t.flags & 1u))
+                ok[q] = in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2);
+            idx[q] = 0;
+            if (ok[q]) {
+                const uint32_t b2 = s2 & p.in_mask;
+                idx[q] = __ldg(p.outer_off + (s2 >> p.n_in)) + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+            }
+        }
+        T2 xv[RT];
+#pragma unroll
+        for (int q = 0; q < RT; ++q)
+            if (ok[q]) xv[q] = x[idx[q]];
+#pragma unroll
+        for (int q = 0; q < RT; ++q) {
+            if (!ok[q]) continue;
             A cr, ci;
             term_amp<uint32_t, A>(t, s[q], p.vars, cr, ci);
-            cmac<A>(ar_[q], ai_[q], cr, ci, x[idx], REAL);
+            cmac<A>(ar_[q], ai_[q], cr, ci, xv[q], REAL);
         }
     }
     T2 xd[RT];
