@@ -6,15 +6,18 @@
 // are.  Hubbard and t-J states, which the reference stores interleaved (up
 // electron of site i at bit 2i, down at 2i+1, src/sites/hubbard_site.cpp:11-29),
 // are stored "split": up occupations at bits 0..N-1, down occupations at bits
-// N..2N-1.  Internal order is ascending internal encoding; for spin/fermion
-// it equals the reference's ascending order, for Hubbard/t-J a permutation
-// (ref_of_int) converts at the C ABI.
+// N..2N-1.
 //
 // Ranking (RANK_TABLE).  A state s splits into an outer part a = s >> n_in and
 // an inner part b = s & (2^n_in - 1).  The states with a given a form one
-// contiguous block; rank(s) = outer_off[a] + inner_rank[b], where inner_rank is
-// the combinatorial-number-system rank of b among the inner configurations of
-// its popcount (ascending order is colex order for a fixed popcount).
+// contiguous block, blocks in ascending a; rank(s) = outer_off[a] +
+// inner_rank[b], where inner_rank is the position of b among the inner
+// configurations of its popcount.  Those are ordered by the number of domain
+// walls of b (adjacent inner bits that differ), then by value: rows whose
+// inner nearest-neighbour flip lists have equal lengths sit together, so the
+// threads of a warp walk lists of equal length in the SpMV.  The reference
+// order is ascending states (colex within a class); a permutation
+// (ref_of_int) converts at the C ABI wherever the two differ.
 // RANK_SEARCH (t-J, and very wide spin chains) keeps the sorted internal states
 // and ranks by binary search inside the block of a.
 #include "qkg.hpp"
@@ -143,11 +146,28 @@ Basis::Basis(Model m, int N_, const Sector& s) : model(m), N(N_), sec(s) {
                 inner_state[class_base[c] + fill[c]] = (uint32_t)b;
                 ++fill[c];
             }
+            bool reordered = false;
+            if (n_in >= 3) {
+                const uint32_t wmask = (uint32_t)((1ULL << (n_in - 1)) - 1);
+                auto walls = [wmask](uint32_t b) { return popc((b ^ (b >> 1)) & wmask); };
+                std::vector<uint32_t> colex_state = inner_state, colex_rank = inner_rank;
+                for (int c = 0; c <= n_in; ++c)
+                    std::stable_sort(inner_state.begin() + class_base[c], inner_state.begin() + class_base[c + 1],
+                                     [&](uint32_t x, uint32_t y) { return walls(x) < walls(y); });
+                for (int c = 0; c <= n_in; ++c)
+                    for (uint32_t r = class_base[c]; r < class_base[c + 1]; ++r) inner_rank[inner_state[r]] = r - class_base[c];
+                reordered = inner_state != colex_state;
+                if (reordered && !split) {
+                    ref_inner_rank = std::move(colex_rank);
+                    ref_inner_state = std::move(colex_state);
+                }
+            }
+            inner_reordered_ = reordered;
         }
         outer_off.assign(nout_cfg + 1, 0);
         for (uint64_t a = 0; a < nout_cfg; ++a) outer_off[a + 1] = outer_off[a] + block_size((uint32_t)a);
         dim = outer_off[nout_cfg];
-        permuted = split && N > 1;
+        permuted = (split && N > 1) || (inner_reordered_ && dim > 1);
     } else {
         // t-J: blocks by down configuration a, inner up configurations avoid a.
         outer_off.assign(nout_cfg + 1, 0);
@@ -247,7 +267,8 @@ inline uint64_t hub_count(const Sector& sec, int up_slots, int dn_slots, int up_
 
 int64_t Basis::index_ref(uint64_t s_ref) const {
     if (!contains_ref(s_ref)) return -1;
-    if (!split) return (int64_t)rank_int(s_ref);
+    if (!split && !permuted) return (int64_t)rank_int(s_ref);
+    if (!split) return (int64_t)(outer_off[s_ref >> n_in] + ref_inner_rank[s_ref & in_mask_]);
     if (model == TJ) {
         auto it = std::lower_bound(states_ref.begin(), states_ref.end(), s_ref);
         return it - states_ref.begin();
@@ -264,7 +285,12 @@ int64_t Basis::index_ref(uint64_t s_ref) const {
 
 uint64_t Basis::state_ref(uint64_t i) const {
     QKG_REQUIRE(i < dim, "basis: index out of range");
-    if (!split) return unrank_int(i);
+    if (!split && !permuted) return unrank_int(i);
+    if (!split) {
+        const auto it = std::upper_bound(outer_off.begin(), outer_off.end(), i);
+        const uint64_t a = (uint64_t)(it - outer_off.begin()) - 1;
+        return (a << n_in) | ref_inner_state[class_base[inner_class_of((uint32_t)a)] + (i - outer_off[a])];
+    }
     if (model == TJ) return states_ref[i];
     uint64_t s = 0;
     int up_rem = sec.nup, dn_rem = sec.ndn;
@@ -354,10 +380,11 @@ const DevBasis& Basis::device(int dev) {
     d.inner_rank = c->upload(inner_rank);
     d.inner_state = c->upload(inner_state);
     d.states_int = c->upload(states_int);
-    if (permuted && dim && split && model != TJ && rank_kind == RANK_TABLE && nbits <= 64) {
-        // Hubbard: interleaved reference ranks computed on the device
+    if (permuted && dim && model != TJ && rank_kind == RANK_TABLE && nbits <= 64 && (split || !inner_all)) {
+        // reference ranks computed on the device: interleaved count (Hubbard)
+        // or block offset + colex rank of the inner configuration (spin/fermion)
         void* p = c->alloc(dim * (d.idx32 ? sizeof(uint32_t) : sizeof(uint64_t)));
-        ref_permutation_device(d, sec, work_items(1024), p);
+        ref_permutation_device(d, sec, work_items(1024), split ? nullptr : &ref_inner_rank, p);
         d.ref_of_int = p;
     } else if (permuted && dim) {
         if (d.idx32) {

@@ -453,7 +453,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     __shared__ A s_iamp[2 * kMaxInnerTable];
     __shared__ KTerm<uint32_t, A> s_mixed[kMaxMixedSmem];
     __shared__ A s_dtab[512];
-    __shared__ int s_n;
+    __shared__ uint2 s_mx[kMaxMixedSmem];  // straddling terms possible in this block: (term, target block offset)
+    __shared__ int s_n, s_nmx;
     const bool mixed_smem = p.n_mixed <= kMaxMixedSmem;
     if (mixed_smem)
         for (int t = threadIdx.x; t < p.n_mixed; t += blockDim.x) s_mixed[t] = p.mixed[t];
@@ -499,21 +500,44 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
             base += __popc(m);
         }
         if (threadIdx.x == 0) s_n = base;
+    } else if (threadIdx.x < 64 && mixed_smem) {
+        // straddling terms whose outer-bit condition holds in this block, with
+        // the offset of the (uniform) target block
+        const uint32_t lane = threadIdx.x - 32u, sa = it.a << p.n_in, omask = ~p.in_mask;
+        int base = 0;
+        for (int t0 = 0; t0 < p.n_mixed; t0 += 32) {
+            const int ti = t0 + (int)lane;
+            bool ok = false;
+            uint32_t boff = 0;
+            if (ti < p.n_mixed) {
+                const KTerm<uint32_t, A> t = p.mixed[ti];
+                if ((sa & t.C & omask) == (t.V & omask)) {
+                    ok = true;
+                    boff = __ldg(p.outer_off + ((sa ^ t.X) >> p.n_in));
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (ok) s_mx[base + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)ti, boff);
+            base += __popc(m);
+        }
+        if (lane == 0) s_nmx = base;
     }
     __syncthreads();
     const int nout = s_n;
     const uint32_t rmask = (1u << p.rbits) - 1u;
 
     A dot_hi = 0, dot_lo = 0;
+    // a warp covers RT * 32 consecutive rows: row q of this thread is tbase + 32 q
+    const uint32_t tbase = (threadIdx.x & ~31u) * RT + (threadIdx.x & 31u);
     // passes of kChunk rows (one pass unless a whole outer block is staged)
     for (uint32_t pass = 0; pass < (STAGE ? it.count : 1u); pass += RT * kBlock) {
     uint32_t s[RT], e0[RT], e1[RT];
     A ar_[RT], ai_[RT];
     bool live[RT];
-    const T2* xr = x + (uint32_t)it.row0 + pass + threadIdx.x;  // row q of this thread is xr[q * kBlock]
+    const T2* xr = x + (uint32_t)it.row0 + pass + tbase;  // row q of this thread is xr[q * 32]
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
-        const uint32_t r = pass + threadIdx.x + q * kBlock;
+        const uint32_t r = pass + tbase + q * 32u;
         live[q] = r < it.count;
         const uint32_t rr = live[q] ? r : 0;
         const uint32_t pidx = it.inner_base + rr;
@@ -530,7 +554,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         T2 xv[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q)
-            if (live[q]) xv[q] = xr[q * kBlock + e.delta];
+            if (live[q]) xv[q] = xr[q * 32 + e.delta];
 #pragma unroll
         for (int q = 0; q < RT; ++q) {
             if (!live[q]) continue;
@@ -614,10 +638,12 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         }
     }
 #endif
-    for (int k = 0; k < p.n_mixed; ++k) {
+    const int nmx = mixed_smem ? s_nmx : p.n_mixed;
+    for (int j = 0; j < nmx; ++j) {
         // the four rows' targets first (their rank lookups in flight together),
         // then the gathers, then the sums
-        const KTerm<uint32_t, A> t = mixed[k];
+        const uint2 mk = mixed_smem ? s_mx[j] : make_uint2((uint32_t)j, 0u);
+        const KTerm<uint32_t, A> t = mixed[mk.x];
         uint32_t idx[RT];
         bool ok[RT];
 #pragma unroll
@@ -629,7 +655,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
             idx[q] = 0;
             if (ok[q]) {
                 const uint32_t b2 = s2 & p.in_mask;
-                idx[q] = __ldg(p.outer_off + (s2 >> p.n_in)) + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+                const uint32_t boff = mixed_smem ? mk.y : __ldg(p.outer_off + (s2 >> p.n_in));
+                idx[q] = boff + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
             }
         }
         T2 xv[RT];
@@ -648,7 +675,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     uint32_t dc[RT];
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
-        const uint32_t rl = live[q] ? pass + threadIdx.x + q * kBlock : 0u;
+        const uint32_t rl = live[q] ? pass + tbase + q * 32u : 0u;
         const uint32_t row = (uint32_t)it.row0 + rl;
         dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
                                        : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
@@ -668,7 +695,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         T2 out;
         out.x = (T)(accr * scale);
         out.y = (T)(acci * scale);
-        y[(uint32_t)it.row0 + pass + threadIdx.x + q * kBlock] = out;
+        y[(uint32_t)it.row0 + pass + tbase + q * 32u] = out;
         if (p.apart) {
             ffma_acc(dot_hi, dot_lo, (A)xd[q].x, (A)out.x);
             ffma_acc(dot_hi, dot_lo, (A)xd[q].y, (A)out.y);
@@ -1094,9 +1121,39 @@ __global__ void ref_perm_kernel(const WorkItem* __restrict__ items, const uint32
     (void)N;
 }
 
-void ref_permutation_device(const DevBasis& d, const Sector& sec, const std::vector<WorkItem>& items, void* out) {
-    QKG_REQUIRE(d.split && d.N <= 32 && d.n_in == d.N, "device permutation: split basis with up bits inner");
+// Reference index of each internal row of a spin/fermion basis whose inner
+// classes are reordered: the block offset (blocks are in ascending a in both
+// orders) plus the colex rank of the row's inner configuration.
+__global__ void ref_perm_colex_kernel(const WorkItem* __restrict__ items, const uint32_t* __restrict__ inner_state,
+                                      const uint32_t* __restrict__ colex_rank, const void* outer_off, int idx32,
+                                      void* out) {
+    const WorkItem it = items[blockIdx.x];
+    const uint64_t off = idx32 ? (uint64_t)static_cast<const uint32_t*>(outer_off)[it.a]
+                               : (uint64_t)static_cast<const unsigned long long*>(outer_off)[it.a];
+    for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
+        const uint64_t rank = off + __ldg(colex_rank + __ldg(inner_state + it.inner_base + r));
+        const uint64_t row = it.row0 + r;
+        if (idx32) static_cast<uint32_t*>(out)[row] = (uint32_t)rank;
+        else static_cast<unsigned long long*>(out)[row] = rank;
+    }
+}
+
+void ref_permutation_device(const DevBasis& d, const Sector& sec, const std::vector<WorkItem>& items,
+                            const std::vector<uint32_t>* ref_inner_rank, void* out) {
     if (items.empty()) return;
+    if (ref_inner_rank) {
+        QKG_REQUIRE(!d.split && !d.inner_all && d.inner_state && ref_inner_rank->size() == (1ULL << d.n_in),
+                    "device permutation: colex ranks of every inner configuration");
+        DBuf cr, it;
+        upload_vec(cr, *ref_inner_rank);
+        upload_vec(it, items);
+        ref_perm_colex_kernel<<<(unsigned)items.size(), 256>>>(it.as<WorkItem>(), d.inner_state, cr.as<uint32_t>(),
+                                                               d.outer_off, d.idx32, out);
+        QKG_LAUNCHED();
+        QKG_CUDA(cudaDeviceSynchronize());
+        return;
+    }
+    QKG_REQUIRE(d.split && d.N <= 32 && d.n_in == d.N, "device permutation: split basis with up bits inner");
     std::vector<unsigned long long> tab(33 * 33, 0);
     for (int n = 0; n <= 32; ++n)
         for (int k = 0; k <= n; ++k) tab[n * 33 + k] = binom(n, k);

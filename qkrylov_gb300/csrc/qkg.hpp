@@ -117,6 +117,9 @@ public:
     int total_pop = -1;          // spin/fermion fixed total popcount (inner class = total - pop(a))
     std::vector<uint64_t> outer_off;
     std::vector<uint32_t> inner_rank, inner_state, class_base;
+    // spin/fermion bases whose inner order is not colex: the colex (reference)
+    // rank of each inner configuration and the colex-ordered configurations
+    std::vector<uint32_t> ref_inner_rank, ref_inner_state;
     std::vector<uint64_t> states_int;  // RANK_SEARCH
     std::vector<uint64_t> states_ref;  // t-J only: sorted reference-encoded states
 
@@ -141,6 +144,7 @@ public:
     const DevBasis& device(int dev);
 
 private:
+    bool inner_reordered_ = false;  // inner classes are not in colex order
     struct DevCopy;
     std::mutex mu_;
     std::vector<std::unique_ptr<DevCopy>> dev_;
@@ -148,9 +152,12 @@ private:
 
 uint64_t binom(int n, int k);
 
-// Reference index of every internal index of a split (Hubbard) basis, computed
-// on the device from the work items (out: uint32 when idx32, else uint64).
-void ref_permutation_device(const DevBasis& d, const Sector& sec, const std::vector<WorkItem>& items, void* out);
+// Reference index of every internal index, computed on the device from the
+// work items (out: uint32 when idx32, else uint64).  Split (Hubbard) bases use
+// the interleaved count; spin/fermion bases pass the colex rank of each inner
+// configuration (ref_inner_rank, 2^n_in entries).
+void ref_permutation_device(const DevBasis& d, const Sector& sec, const std::vector<WorkItem>& items,
+                            const std::vector<uint32_t>* ref_inner_rank, void* out);
 
 // ---------------------------------------------------------------- operators
 struct Factor { std::string op; int site; };
