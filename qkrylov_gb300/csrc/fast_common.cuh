@@ -95,11 +95,10 @@ struct FastParams {
     int n_dtab;
     const void* dcode;
     const A* dtab;
-    // Lanczos mode (all null otherwise): x = vtab[*kstep], y = vtab[*kstep + 1],
-    // y is scaled by sig[*kstep], and each block writes Re sum conj(x) y to apart.
-    const void* const* vtab;
-    const int* kstep;
-    const double* sig;
+    // Lanczos mode (null otherwise): x, y, scale and the previous-vector term
+    // from *lz (y = scale H x - bprev vprev); each block writes Re sum conj(x) y
+    // to apart.
+    const LzOperands* lz;
     double2* apart;
 };
 
@@ -113,6 +112,38 @@ __device__ __forceinline__ void ffma_acc(float& hi, float& lo, float a, float b)
     hi = t;
 }
 __device__ __forceinline__ void ffma_acc(double& hi, double& lo, double a, double b) { hi = fma(a, b, hi); }
+
+// (hi, lo) += (bh, bl) in float-float arithmetic (TwoSum on the high parts).
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl) {
+    const float t = hi + bh;
+    const float z = t - hi;
+    lo += ((hi - (t - z)) + (bh - z)) + bl;
+    hi = t;
+}
+// Block sum of float-float values, entirely in FP32 arithmetic (the FP64 pipe
+// is narrow: a double-precision block reduction in every small CTA costs more
+// than the reduction is worth).  The result is valid in thread 0.
+__device__ __forceinline__ float2 block_sum_ff(float hi, float lo) {
+    __shared__ float2 shf[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const float bh = __shfl_down_sync(0xffffffffu, hi, o), bl = __shfl_down_sync(0xffffffffu, lo, o);
+        ff_add(hi, lo, bh, bl);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) shf[wid] = make_float2(hi, lo);
+    __syncthreads();
+    if (wid == 0) {
+        const float2 v = (threadIdx.x < (blockDim.x >> 5)) ? shf[lane] : make_float2(0.f, 0.f);
+        hi = v.x;
+        lo = v.y;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float bh = __shfl_down_sync(0xffffffffu, hi, o), bl = __shfl_down_sync(0xffffffffu, lo, o);
+            ff_add(hi, lo, bh, bl);
+        }
+    }
+    return make_float2(hi, lo);
+}
 
 __device__ __forceinline__ double block_sum_d(double v) {
     __shared__ double sh[32];

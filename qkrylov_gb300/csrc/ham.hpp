@@ -38,11 +38,19 @@ constexpr int kFastVariants = 5;
 // Device-resident Lanczos step: the SpMV reads its vectors through a device
 // pointer table indexed by a device step counter (x = vtab[k], y = vtab[k+1]),
 // scales y by sig[k] and writes one Re<x, y> partial per block to apart.
+// Operands of one Lanczos-mode SpMV, kept in device memory and rewritten by
+// the step's last kernel for the next step: y = scale H x - bprev vprev
+// (vprev null: no previous-vector term).
+struct LzOperands {
+    const void* x = nullptr;
+    void* y = nullptr;
+    const void* vprev = nullptr;
+    double scale = 1.0, bprev = 0.0;
+    float scale32 = 1.f, bprev32 = 0.f;  // the same, rounded once for FP32 kernels
+};
 struct LanczosHooks {
-    const void* const* vtab = nullptr;
-    const int* kstep = nullptr;
-    const double* sig = nullptr;
-    double2* apart = nullptr;
+    const LzOperands* op = nullptr;  // device
+    double2* apart = nullptr;        // per-block partials of Re<x, y>
 };
 
 namespace fastk {

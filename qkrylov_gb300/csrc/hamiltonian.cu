@@ -270,12 +270,15 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
     T2* xs = reinterpret_cast<T2*>(fast_smem);
     const T2* __restrict__ x = x_in;
     T2* __restrict__ y = y_in;
-    A scale = (A)1;
-    if (p.vtab) {
-        const int k = *p.kstep;
-        x = static_cast<const T2*>(p.vtab[k]);
-        y = static_cast<T2*>(const_cast<void*>(p.vtab[k + 1]));
-        scale = (A)p.sig[k];
+    A scale = (A)1, bprev = (A)0;
+    const T2* __restrict__ vprev = nullptr;
+    if (p.lz) {
+        const LzOperands o = *p.lz;
+        x = static_cast<const T2*>(o.x);
+        y = static_cast<T2*>(o.y);
+        vprev = static_cast<const T2*>(o.vprev);
+        scale = sizeof(A) == 4 ? (A)o.scale32 : (A)o.scale;  // no per-thread FP64 conversion for FP32
+        bprev = sizeof(A) == 4 ? (A)o.bprev32 : (A)o.bprev;
     }
     A dot_hi = 0, dot_lo = 0;  // Re sum conj(x) y over this thread's rows (Lanczos mode)
     __shared__ OutEnt<A> s_out[kMaxOuter];
@@ -396,9 +399,15 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
                 acci = fma(di, (A)xd.x, acci);
             }
         }
+        A o_r = accr * scale, o_i = acci * scale;
+        if (vprev) {
+            const T2 pv = vprev[row];
+            o_r = fma(-bprev, (A)pv.x, o_r);
+            o_i = fma(-bprev, (A)pv.y, o_i);
+        }
         T2 out;
-        out.x = (T)(accr * scale);
-        out.y = (T)(acci * scale);
+        out.x = (T)o_r;
+        out.y = (T)o_i;
         y[row] = out;
         if (p.apart) {
             ffma_acc(dot_hi, dot_lo, (A)xd.x, (A)out.x);
@@ -406,16 +415,22 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
         }
     }
     if (p.apart) {
-        const double s = block_sum_d((double)dot_hi + (double)dot_lo);
-        if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2(s, 0.0);
+        if (sizeof(A) == 4) {
+            const float2 t = block_sum_ff((float)dot_hi, (float)dot_lo);
+            if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2((double)t.x + (double)t.y, 0.0);
+        } else {
+            const double t = block_sum_d((double)dot_hi + (double)dot_lo);
+            if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2(t, 0.0);
+        }
     }
 }
 
-// Unstaged fast kernel, four rows per thread: a 1024-row work item gives
-// thread t the rows t, t+256, t+512, t+768.  Every outer entry and every
-// straddling term is read once per thread and applied to its four rows, which
-// also gives four independent gathers in flight per entry; the four rows'
-// ELL walks advance together.
+// Unstaged fast kernel, four rows per thread: in a 1024-row work item warp w
+// covers rows 128w .. 128w+127, lane l taking rows 128w + l + 32q (q < 4), so
+// row q of every lane lies in one 32-row ELL group.  Every outer entry and
+// every straddling term is read once per thread and applied to its four rows,
+// which also gives four independent gathers in flight per entry; the four
+// rows' ELL walks advance together.
 constexpr int kRowsPerThread = 4;
 static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread rows per thread");
 
@@ -442,12 +457,15 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     T2* xs = reinterpret_cast<T2*>(rows_smem);  // STAGE: the outer block's slice of x
     const T2* __restrict__ x = x_in;
     T2* __restrict__ y = y_in;
-    A scale = (A)1;
-    if (p.vtab) {
-        const int k = *p.kstep;
-        x = static_cast<const T2*>(p.vtab[k]);
-        y = static_cast<T2*>(const_cast<void*>(p.vtab[k + 1]));
-        scale = (A)p.sig[k];
+    A scale = (A)1, bprev = (A)0;
+    const T2* __restrict__ vprev = nullptr;
+    if (p.lz) {
+        const LzOperands o = *p.lz;
+        x = static_cast<const T2*>(o.x);
+        y = static_cast<T2*>(o.y);
+        vprev = static_cast<const T2*>(o.vprev);
+        scale = sizeof(A) == 4 ? (A)o.scale32 : (A)o.scale;  // no per-thread FP64 conversion for FP32
+        bprev = sizeof(A) == 4 ? (A)o.bprev32 : (A)o.bprev;
     }
     __shared__ OutEnt<A> s_out[kMaxOuter];
     __shared__ A s_iamp[2 * kMaxInnerTable];
@@ -671,7 +689,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
             cmac<A>(ar_[q], ai_[q], cr, ci, xv[q], REAL);
         }
     }
-    T2 xd[RT];
+    T2 xd[RT], pv[RT];
     uint32_t dc[RT];
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
@@ -680,6 +698,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
                                        : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
         xd[q] = STAGE ? xs[rl] : x[row];
+        if (vprev) pv[q] = vprev[row];
     }
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
@@ -692,9 +711,14 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
             accr = fma(-di, (A)xd[q].y, accr);
             acci = fma(di, (A)xd[q].x, acci);
         }
+        A o_r = accr * scale, o_i = acci * scale;
+        if (vprev) {
+            o_r = fma(-bprev, (A)pv[q].x, o_r);
+            o_i = fma(-bprev, (A)pv[q].y, o_i);
+        }
         T2 out;
-        out.x = (T)(accr * scale);
-        out.y = (T)(acci * scale);
+        out.x = (T)o_r;
+        out.y = (T)o_i;
         y[(uint32_t)it.row0 + pass + tbase + q * 32u] = out;
         if (p.apart) {
             ffma_acc(dot_hi, dot_lo, (A)xd[q].x, (A)out.x);
@@ -703,8 +727,13 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     }
     }
     if (p.apart) {
-        const double sum = block_sum_d((double)dot_hi + (double)dot_lo);
-        if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2(sum, 0.0);
+        if (sizeof(A) == 4) {
+            const float2 t = block_sum_ff((float)dot_hi, (float)dot_lo);
+            if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2((double)t.x + (double)t.y, 0.0);
+        } else {
+            const double t = block_sum_d((double)dot_hi + (double)dot_lo);
+            if (threadIdx.x == 0) p.apart[blockIdx.x] = make_double2(t, 0.0);
+        }
     }
 }
 
@@ -1439,9 +1468,7 @@ void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) cons
     fast_params(p);
     size_t ni = 0;
     p.items = items_of(v, &ni);
-    p.vtab = lz.vtab;
-    p.kstep = lz.kstep;
-    p.sig = lz.sig;
+    p.lz = lz.op;
     p.apart = lz.apart;
     launch_fast<float, float>(p, ni, all_real_, unif_, nullptr, nullptr, s, v, st ? max_block_ * 8 : 0);
 }

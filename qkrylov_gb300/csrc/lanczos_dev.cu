@@ -6,10 +6,14 @@
 // V_{k+1} = w_k (the un-normalised residual of step k), sig[k+1] = 1 / beta_k.
 // The SpMV multiplies its output by sig[k], so y = H v_k and every stored
 // vector has norm beta_{k-1}: no growth, no separate normalisation pass.
-//   1. SpMV (fast kernel, Lanczos mode): V_{k+1} = sig_k H V_k, plus per-block
-//      partials of Re<V_k, V_{k+1}>  =>  alpha_k = sig_k * sum.
-//   2. lz_alpha: alpha_k; coefficients a = alpha_k sig_k, b = beta_{k-1} sig_{k-1}.
-//   3. lz_update: V_{k+1} -= a V_k + b V_{k-1}; compensated |V_{k+1}|^2 partials.
+//   1. SpMV (fast kernel, Lanczos mode): V_{k+1} = sig_k H V_k - beta_{k-1}
+//      sig_{k-1} V_{k-1} (the previous-vector term applied as each row is
+//      written), plus per-block partials of Re<V_k, V_{k+1}>  =>  alpha_k =
+//      sig_k * sum = <v_k, H v_k - beta_{k-1} v_{k-1}> (the modified
+//      Gram-Schmidt order of Paige's Lanczos variant: equal to <v_k, H v_k> in
+//      exact arithmetic, one pass over a vector fewer per step).
+//   2. lz_alpha: alpha_k and the coefficient a = alpha_k sig_k.
+//   3. lz_update: V_{k+1} -= a V_k; compensated |V_{k+1}|^2 partials.
 //      (selective reorthogonalisation adds lz_proj, lz_proj_finish, lz_orth)
 //   4. lz_beta: beta_k, sig_{k+1}, k += 1.
 // alpha/beta are also written to mapped pinned host memory; the host reads
@@ -93,7 +97,7 @@ __global__ void lz_alpha_kernel(const double2* __restrict__ apart, int nparts, L
         alpha[k] = a;
         alpha_host[k] = a;
         st->a = a * sig[k];
-        st->b = k > 0 ? beta[k - 1] * sig[k - 1] : 0.0;
+        st->b = 0.0;  // the SpMV already subtracted beta_{k-1} v_{k-1}
         *arrived = 0u;  // ready for the next step
     }
 }
@@ -123,7 +127,8 @@ __device__ __forceinline__ float2 upd_elem(float2 x, float2 c, float2 d, float2 
     return x;
 }
 
-// w -= a v + b v_prev in place, ||w||^2 partials (and <psi, w> partials with
+// w -= a v + b v_prev in place (b = 0: the SpMV applied the previous-vector
+// term, and v_prev is not read), ||w||^2 partials (and <psi, w> partials with
 // PROJ, for selective reorthogonalisation): two elements per thread and
 // iteration with 16-byte accesses (the Krylov vectors are 256-byte aligned).
 template <bool PROJ>
@@ -133,16 +138,17 @@ __global__ void lz_update_t(void* const* __restrict__ vtab, const LzState* __res
     const int k = st->k;
     float2* __restrict__ w = static_cast<float2*>(vtab[k + 1]);
     const float2* __restrict__ v = static_cast<const float2*>(vtab[k]);
-    const float2* __restrict__ vp = k > 0 ? static_cast<const float2*>(vtab[k - 1]) : v;
-    const bool has_prev = k > 0;
     const float a = (float)st->a, b = (float)st->b;
+    const bool has_prev = k > 0 && b != 0.f;
+    const float2* __restrict__ vp = has_prev ? static_cast<const float2*>(vtab[k - 1]) : v;
     UpdAcc s;
     const uint64_t n2 = n / 2, step = (uint64_t)gridDim.x * blockDim.x;
     const float2 zero = make_float2(0.f, 0.f);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n2; i += step) {
         const float4 x4 = reinterpret_cast<const float4*>(w)[i];
         const float4 c4 = reinterpret_cast<const float4*>(v)[i];
-        const float4 d4 = reinterpret_cast<const float4*>(vp)[i];
+        float4 d4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (has_prev) d4 = reinterpret_cast<const float4*>(vp)[i];
         float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (PROJ) p4 = reinterpret_cast<const float4*>(psi)[i];
         const float2 y0 = upd_elem<PROJ>(make_float2(x4.x, x4.y), make_float2(c4.x, c4.y), make_float2(d4.x, d4.y),
@@ -200,18 +206,30 @@ __global__ void lz_orth_kernel(void* const* __restrict__ vtab, const LzState* __
     if (threadIdx.x == 0) bpart[blockIdx.x] = s;
 }
 
+// beta_k, sig_{k+1}, k += 1, and the next step's SpMV operands:
+// y = sig_{k+1} H V_{k+1} - beta_k sig_k V_k into V_{k+2}.
 __global__ void lz_beta_kernel(const double2* __restrict__ bpart, int nparts, LzState* st, double* beta, double* sig,
-                               double* beta_host) {
+                               double* beta_host, void* const* __restrict__ vtab, int nmax, LzOperands* op) {
     double s = 0.0;
     for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += bpart[i].x;
     const double2 t = bsum2(s, 0.0);
     if (threadIdx.x == 0) {
         const int k = st->k;
         const double b = sqrt(t.x);
+        const double sn = b > 0.0 ? 1.0 / b : 0.0;
         beta[k] = b;
         beta_host[k] = b;
-        sig[k + 1] = b > 0.0 ? 1.0 / b : 0.0;
+        sig[k + 1] = sn;
         st->k = k + 1;
+        LzOperands o;
+        o.x = vtab[min(k + 1, nmax)];
+        o.y = vtab[min(k + 2, nmax)];  // no step runs past nmax - 1
+        o.vprev = vtab[k];
+        o.scale = sn;
+        o.bprev = b * sig[k];
+        o.scale32 = (float)o.scale;
+        o.bprev32 = (float)o.bprev;
+        *op = o;
     }
 }
 
@@ -288,18 +306,21 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     }
     const double nr0 = std::sqrt(nrm2sq_f32(v0, n, ws, st));
     if (nr0 != 0.0) scal_f32(1.0 / nr0, v0, n, st);
+    DBuf lzop(sizeof(LzOperands));
     {
         LzState s0{};
         const double one = 1.0;
+        LzOperands op0;  // step 0: y = H v_0, no previous vector
+        op0.x = vptr[0];
+        op0.y = vptr[1];
         QKG_CUDA(cudaMemcpyAsync(state.p, &s0, sizeof(s0), cudaMemcpyHostToDevice, st));
         QKG_CUDA(cudaMemcpyAsync(sig.p, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+        QKG_CUDA(cudaMemcpyAsync(lzop.p, &op0, sizeof(op0), cudaMemcpyHostToDevice, st));
         QKG_CUDA(cudaStreamSynchronize(st));
     }
 
     LanczosHooks hooks;
-    hooks.vtab = static_cast<const void* const*>(vtab.p);
-    hooks.kstep = &state.as<LzState>()->k;
-    hooks.sig = sig.as<double>();
+    hooks.op = lzop.as<LzOperands>();
     hooks.apart = apart.as<double2>();
     const int nparts = (int)H.lanczos_parts();
     DBuf psi;  // selective reorthogonalisation vector (once active)
@@ -327,7 +348,8 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
             QKG_LAUNCHED();
         }
         lz_beta_kernel<<<1, kT, 0, st>>>(bpart.as<double2>(), kUpdGrid, state.as<LzState>(), beta.as<double>(),
-                                         sig.as<double>(), bh.d);
+                                         sig.as<double>(), bh.d, static_cast<void* const*>(vtab.p), nmax,
+                                         lzop.as<LzOperands>());
         QKG_LAUNCHED();
     };
     int kernels_plain = 0, kernels_so = 0;  // kernels per step graph, counted at capture
