@@ -300,6 +300,11 @@ int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, 
  * bit encoding (qkrylov_basis_state for a range). */
 int qkrylov_basis_states(qkrylov_basis_h basis, uint64_t first, uint64_t count, uint64_t* out);
 
+/* Device memory the Hamiltonian keeps between solver calls (the FP32 Krylov
+ * space of the mixed Lanczos: maxiter + 7 vectors): *bytes receives its size;
+ * release != 0 frees it now (it is also freed with the Hamiltonian). */
+int qkrylov_hamiltonian_workspace(qkrylov_hamiltonian_h h, int release, uint64_t* bytes);
+
 /* Time `reps` back-to-back applies of the FP32 (fp32 != 0) or FP64 kernel on
  * internal device vectors, with CUDA events on the Hamiltonian's stream;
  * *ms_per_apply receives the mean launch duration. */

@@ -131,6 +131,7 @@ _SIGS = {
     "qkrylov_basis_states": (_i, [_vp, _u64, _u64, _u64p]),
     "qkrylov_davidson_lowest_ex": (_i, [_vp, _i, _i, _d, _i, _i, _dp, _dp, _dp, _vp, _dp]),
     "qkrylov_hamiltonian_benchmark_apply": (_i, [_vp, _i, _i, _dp]),
+    "qkrylov_hamiltonian_workspace": (_i, [_vp, _i, _u64p]),
 }
 
 _lib = None
@@ -388,6 +389,13 @@ class MatrixFreeHamiltonian(_Handle):
         f = _c.c_int()
         _check(lib().qkrylov_hamiltonian_select_kernel(self._h, m, _c.byref(f)))
         return bool(f.value)
+
+    def workspace_bytes(self, release=False):
+        """Device memory kept for the next solver call (the mixed Lanczos
+        Krylov space); release=True frees it first."""
+        b = _c.c_uint64()
+        _check(lib().qkrylov_hamiltonian_workspace(self._h, int(bool(release)), _c.byref(b)))
+        return b.value
 
     def tuning(self, fp32=True):
         """(variant, {variant: autotuned ms}) of the fast kernel used in mode 0;

@@ -408,6 +408,15 @@ int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, 
     return QKRYLOV_SUCCESS;
 }
 
+int qkrylov_hamiltonian_workspace(qkrylov_hamiltonian_h h, int release, uint64_t* bytes) {
+    if (!h || !h->ptr) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        set_device(h);
+        if (release) h->ptr->release_workspace();
+        if (bytes) *bytes = h->ptr->workspace_bytes();
+    });
+}
+
 int qkrylov_hamiltonian_benchmark_apply(qkrylov_hamiltonian_h h, int fp32, int reps, double* ms) {
     if (!h || !h->ptr || !ms || reps <= 0) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {

@@ -35,12 +35,10 @@ enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
 enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3, FV_ROWS4_WIDE = 4 };
 constexpr int kFastVariants = 5;
 
-// Device-resident Lanczos step: the SpMV reads its vectors through a device
-// pointer table indexed by a device step counter (x = vtab[k], y = vtab[k+1]),
-// scales y by sig[k] and writes one Re<x, y> partial per block to apart.
-// Operands of one Lanczos-mode SpMV, kept in device memory and rewritten by
-// the step's last kernel for the next step: y = scale H x - bprev vprev
-// (vprev null: no previous-vector term).
+// Device-resident Lanczos step.  The operands of one Lanczos-mode SpMV are kept
+// in device memory and rewritten by the step's last kernel for the next step:
+// y = scale H x - bprev vprev (vprev null: no previous-vector term); the SpMV
+// writes one Re<x, y> partial per block to apart.
 struct LzOperands {
     const void* x = nullptr;
     void* y = nullptr;
@@ -143,6 +141,14 @@ public:
     size_t lanczos_parts() const;  // partial sums written by apply_lanczos_f32
     static constexpr size_t kStageLimit = 200 * 1024;
 
+    // Device memory kept between solver calls on this Hamiltonian (the Krylov
+    // space of the device-resident Lanczos, tens of GB): cudaFree of 64 GB
+    // takes about 25 ms, a tenth of a 200-step run.  Grows on demand, contents
+    // undefined; released with the Hamiltonian or by release_workspace().
+    DBuf& krylov_workspace(size_t bytes) const;
+    void release_workspace() const { kws_.reset(); }
+    size_t workspace_bytes() const { return kws_.bytes; }
+
 private:
     void build_diagonal();
     void build_fast();
@@ -182,6 +188,7 @@ private:
     int diag_mode_ = DIAG_U8;
     DBuf dcode_, dtab64_, dtab32_, dfull64_, dfull32_;
     int n_dtab_ = 0;
+    mutable DBuf kws_;
 };
 
 // ------------------------------------------------------------ Krylov algebra

@@ -1234,6 +1234,14 @@ void Hamiltonian::fast_params(FastParams<A>& p) const {
     p.dtab = dtab.as<A>();
 }
 template void Hamiltonian::fast_params<float>(FastParams<float>&) const;
+DBuf& Hamiltonian::krylov_workspace(size_t bytes) const {
+    if (kws_.bytes < bytes) {
+        kws_.reset();  // free first: the old and new spaces need not fit together
+        kws_.alloc(bytes);
+    }
+    return kws_;
+}
+
 std::vector<WorkItem> Hamiltonian::items_host() const {
     std::vector<WorkItem> v(n_items_);
     if (n_items_) QKG_CUDA(cudaMemcpy(v.data(), items_.p, n_items_ * sizeof(WorkItem), cudaMemcpyDeviceToHost));

@@ -258,18 +258,30 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
     if (nmax <= 0) return out;
     // all nmax + 1 Krylov vectors (FP32) up front: the graph addresses them through vtab
-    size_t fr = 0, tot = 0;
-    QKG_CUDA(cudaMemGetInfo(&fr, &tot));
     // vectors start on 256-byte boundaries (a warp's 32 consecutive rows then
     // cover whole 128-byte lines)
     const uint64_t stride = (n + 31) / 32 * 32;
-    const size_t need = (size_t)(nmax + 1) * stride * sizeof(float2);
-    if (need + (512ull << 20) > fr)
-        throw Error(CUDA_ERR, "out of device memory for " + std::to_string(nmax + 1) + " Krylov vectors");
-    // one allocation for all vectors (a cudaMalloc per vector costs more than a step)
-    DBuf V(need);
+    // workspace: nmax + 1 Krylov vectors, then psi (FP32), the Ritz vector
+    // (FP32), the refined Ritz vector and its residual (FP64); the FP64 slots
+    // also stage a caller's start vector, psi and the FP32 Ritz slot together
+    // the reference-order copy of the eigenvector
+    const size_t need = (size_t)(nmax + 1 + 6) * stride * sizeof(float2);
+    if (H.workspace_bytes() < need) {
+        H.release_workspace();
+        size_t fr = 0, tot = 0;
+        QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+        if (need + (512ull << 20) > fr)
+            throw Error(CUDA_ERR, "out of device memory for " + std::to_string(nmax + 1) + " Krylov vectors");
+    }
+    // one allocation for all vectors (a cudaMalloc per vector costs more than a
+    // step), kept on the Hamiltonian for the next run
+    const DBuf& V = H.krylov_workspace(need);
     std::vector<void*> vptr;
     for (int i = 0; i <= nmax; ++i) vptr.push_back(V.as<float2>() + (size_t)i * stride);
+    float2* const psi_p = V.as<float2>() + (size_t)(nmax + 1) * stride;
+    float2* const r32_p = psi_p + stride;
+    double2* const r64_p = reinterpret_cast<double2*>(r32_p + stride);
+    double2* const h64_p = r64_p + stride;
     DBuf vtab((nmax + 1) * sizeof(void*));
     QKG_CUDA(cudaMemcpy(vtab.p, vptr.data(), vptr.size() * sizeof(void*), cudaMemcpyHostToDevice));
     DBuf state(sizeof(LzState)), alpha((nmax + 2) * 8), beta((nmax + 2) * 8), sig((nmax + 2) * 8);
@@ -293,13 +305,11 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
             ref_uniform_complex(1234, n, h.data(), o.f32_stream);
             src = h.data();
         }
-        DBuf t64(n * sizeof(double2)), d64;
-        QKG_CUDA(cudaMemcpyAsync(t64.p, src, n * sizeof(double2), cudaMemcpyHostToDevice, st));
-        const double2* in = t64.as<double2>();
+        QKG_CUDA(cudaMemcpyAsync(r64_p, src, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+        const double2* in = r64_p;
         if (H.permuted()) {
-            d64.alloc(n * sizeof(double2));
-            H.to_internal_f64(t64.as<double2>(), d64.as<double2>(), st);
-            in = d64.as<double2>();
+            H.to_internal_f64(r64_p, h64_p, st);
+            in = h64_p;
         }
         f64_to_f32(in, v0, n, st);
         QKG_CUDA(cudaStreamSynchronize(st));
@@ -323,7 +333,7 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     hooks.op = lzop.as<LzOperands>();
     hooks.apart = apart.as<double2>();
     const int nparts = (int)H.lanczos_parts();
-    DBuf psi;  // selective reorthogonalisation vector (once active)
+    float2* psi = nullptr;  // selective reorthogonalisation vector (once active)
     auto enqueue_step = [&](bool so, LaunchTimer* timer) {
         if (timer) timer->start();
         H.apply_lanczos_f32(hooks, st);
@@ -338,13 +348,13 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
             QKG_LAUNCHED();
         } else {
             lz_update_t<true><<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
-                                                       psi.as<float2>(), bpart.as<double2>(), ppart.as<double2>());
+                                                       psi, bpart.as<double2>(), ppart.as<double2>());
             QKG_LAUNCHED();
             lz_proj_finish_kernel<<<1, kT, 0, st>>>(ppart.as<double2>(), bpart.as<double2>(), kUpdGrid,
                                                     state.as<LzState>(), kOrthTol);
             QKG_LAUNCHED();
             lz_orth_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(),
-                                                    psi.as<float2>(), n, bpart.as<double2>());
+                                                    psi, n, bpart.as<double2>());
             QKG_LAUNCHED();
         }
         lz_beta_kernel<<<1, kT, 0, st>>>(bpart.as<double2>(), kUpdGrid, state.as<LzState>(), beta.as<double>(),
@@ -406,12 +416,12 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
                             c[i] = s[i] * sg;
                             sg = 1.0 / bh.h[i];
                         }
-                        psi.alloc(n * sizeof(float2));
-                        QKG_CUDA(cudaMemsetAsync(psi.p, 0, n * sizeof(float2), st));
-                        mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), j + 1, c.data(), psi.as<float2>(),
+                        psi = psi_p;
+                        QKG_CUDA(cudaMemsetAsync(psi, 0, n * sizeof(float2), st));
+                        mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), j + 1, c.data(), psi,
                                      n, ws, st);
-                        const double pn = std::sqrt(nrm2sq_f32(psi.as<float2>(), n, ws, st));
-                        scal_f32(1.0 / pn, psi.as<float2>(), n, st);
+                        const double pn = std::sqrt(nrm2sq_f32(psi, n, ws, st));
+                        scal_f32(1.0 / pn, psi, n, st);
                         so_active = true;
                     }
                 }
@@ -473,16 +483,15 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
         c[i] = s[i] * sg;
         sg = 1.0 / bh.h[i];
     }
-    DBuf r32(n * sizeof(float2)), r64(n * sizeof(double2)), h64(n * sizeof(double2));
-    QKG_CUDA(cudaMemsetAsync(r32.p, 0, n * sizeof(float2), st));
-    mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), (int)c.size(), c.data(), r32.as<float2>(), n, ws, st);
-    f32_to_f64(r32.as<float2>(), r64.as<double2>(), n, st);
-    const double nr = std::sqrt(nrm2sq_f64(r64.as<double2>(), n, ws, st));
-    scal_f64(1.0 / nr, r64.as<double2>(), n, st);
-    H.apply_f64(r64.as<double2>(), h64.as<double2>(), st);
-    const double E = dot_f64(r64.as<double2>(), h64.as<double2>(), n, ws, st).real();
-    axpy_f64(-E, r64.as<double2>(), h64.as<double2>(), n, st);
-    out.residual = std::sqrt(nrm2sq_f64(h64.as<double2>(), n, ws, st));
+    QKG_CUDA(cudaMemsetAsync(r32_p, 0, n * sizeof(float2), st));
+    mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), (int)c.size(), c.data(), r32_p, n, ws, st);
+    f32_to_f64(r32_p, r64_p, n, st);
+    const double nr = std::sqrt(nrm2sq_f64(r64_p, n, ws, st));
+    scal_f64(1.0 / nr, r64_p, n, st);
+    H.apply_f64(r64_p, h64_p, st);
+    const double E = dot_f64(r64_p, h64_p, n, ws, st).real();
+    axpy_f64(-E, r64_p, h64_p, n, st);
+    out.residual = std::sqrt(nrm2sq_f64(h64_p, n, ws, st));
     out.energy = E;
     out.t_refine = secs(t1, clk::now());
     if (o.want_vec) {
@@ -491,12 +500,11 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
             out.evec.resize(n);
             dst = out.evec.data();
         }
-        DBuf t2;
-        const double2* src = r64.as<double2>();
+        const double2* src = r64_p;
         if (H.permuted()) {
-            t2.alloc(n * sizeof(double2));
-            H.to_reference_f64(r64.as<double2>(), t2.as<double2>(), st);
-            src = t2.as<double2>();
+            double2* t2 = reinterpret_cast<double2*>(psi_p);  // psi and the FP32 Ritz slot, no longer needed
+            H.to_reference_f64(r64_p, t2, st);
+            src = t2;
         }
         QKG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
         QKG_CUDA(cudaStreamSynchronize(st));

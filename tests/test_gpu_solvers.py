@@ -155,6 +155,27 @@ def test_mixed_device_engine_matches_host_driven(qk, m):
     assert abs(f.energy - r64.energy) <= 1e-10 * abs(r64.energy)
 
 
+def test_krylov_workspace_reused_across_runs(qk):
+    """The mixed Lanczos keeps its Krylov space on the Hamiltonian: a second
+    run with the same seed reuses it (no fresh allocation) and reproduces the
+    first bit for bit (nothing depends on the stale contents); a shorter run
+    fits in it; release frees it."""
+    b, s, o = make_model(qk, *M.heisenberg(18, True, 0))
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    assert H.workspace_bytes() == 0
+    f1 = qk.lanczos_fixed_steps(H, 40, seed=5, mixed=True)
+    nbytes = H.workspace_bytes()
+    stride = (H.dimension + 31) // 32 * 32
+    assert nbytes == (40 + 1 + 6) * stride * 8
+    f2 = qk.lanczos_fixed_steps(H, 40, seed=5, mixed=True)
+    assert H.workspace_bytes() == nbytes
+    assert (f1.energy, f1.energy_tridiag, f1.residual) == (f2.energy, f2.energy_tridiag, f2.residual)
+    f3 = qk.lanczos_fixed_steps(H, 20, seed=5, mixed=True)
+    assert H.workspace_bytes() == nbytes and f3.iterations == 20
+    assert f3.energy_tridiag > f1.energy_tridiag - 1e-12  # fewer steps: a Ritz value no lower
+    assert H.workspace_bytes(release=True) == 0
+
+
 def test_lanczos_from_given_start_matches_oracle(qk, oracle):
     """Same start vector on both sides: E0 and iteration count of the
     reference algorithm (oracle restatement) are reproduced."""
