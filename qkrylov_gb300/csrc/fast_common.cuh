@@ -91,6 +91,13 @@ struct FastParams {
     const KTerm<uint32_t, A>* mixed;
     const KVar<A>* vars;
     int n_mixed;
+    // per outer configuration a: its valid outer entries oent[optr[a] ..
+    // optr[a+1]) and the straddling terms whose outer-bit condition holds,
+    // ment[mptr[a] .. mptr[a+1]) = (term index, target block offset)
+    const uint32_t* optr;
+    const OutEnt<A>* oent;
+    const uint32_t* mptr;
+    const uint2* ment;
     int diag_mode;
     int n_dtab;
     const void* dcode;

@@ -157,6 +157,7 @@ private:
     // fast-path data (see spmv_fast_kernel)
     struct FastSet {
         DBuf outer, inner, mixed, vars;
+        DBuf oent;  // per-block outer entries (OutEnt of this precision)
         int n_outer = 0, n_inner = 0, n_mixed = 0, outer_has_j = 0;
     };
     void autotune();
@@ -173,6 +174,7 @@ private:
     size_t n_ient_ = 0;
     FastSet f64s_, f32s_;
     DBuf iptr_, ient_;
+    DBuf optr_, mptr_, ment_;  // per-block outer-entry / straddling-term list offsets and straddling entries
 
     std::shared_ptr<Basis> basis_;
     const DevBasis* db_ = nullptr;

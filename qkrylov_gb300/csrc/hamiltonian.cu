@@ -281,17 +281,7 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
         bprev = sizeof(A) == 4 ? (A)o.bprev32 : (A)o.bprev;
     }
     A dot_hi = 0, dot_lo = 0;  // Re sum conj(x) y over this thread's rows (Lanczos mode)
-    __shared__ OutEnt<A> s_out[kMaxOuter];
     __shared__ A s_iamp[2 * kMaxInnerTable];
-    __shared__ KTerm<uint32_t, A> s_mixed[kMaxMixedSmem];
-    __shared__ A s_dtab[512];
-    __shared__ int s_n;
-    const bool mixed_smem = p.n_mixed <= kMaxMixedSmem;
-    if (mixed_smem)
-        for (int t = threadIdx.x; t < p.n_mixed; t += blockDim.x) s_mixed[t] = p.mixed[t];
-    if (p.diag_mode == DIAG_U8)  // at most 256 values
-        for (int t = threadIdx.x; t < 2 * p.n_dtab; t += blockDim.x) s_dtab[t] = p.dtab[t];
-    const KTerm<uint32_t, A>* mixed = mixed_smem ? s_mixed : p.mixed;
     const WorkItem it = p.items[blockIdx.x];
     const uint32_t block_off = __ldg(p.outer_off + it.a);
     if (STAGE)  // the item is the whole block: rows [block_off, block_off + count)
@@ -306,36 +296,10 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
             s_iamp[2 * t + 1] = neg ? -k.ai : k.ai;
         }
     }
-    if (threadIdx.x < 32) {
-        // the outer terms valid for this block, in term order
-        const uint32_t b0 = p.inner_state ? __ldg(p.inner_state + it.inner_base) : it.inner_base;
-        const uint32_t s0 = (it.a << p.n_in) | b0;
-        int base = 0;
-        for (int t0 = 0; t0 < p.n_outer; t0 += 32) {
-            const int ti = t0 + (int)threadIdx.x;
-            bool ok = false;
-            OutEnt<A> e;
-            if (ti < p.n_outer) {
-                const KTerm<uint32_t, A> t = p.outer[ti];
-                if ((s0 & t.C) == t.V) {
-                    const uint32_t s2 = s0 ^ t.X;
-                    if (!(t.flags & 1u) || in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2)) {
-                        ok = true;
-                        e.delta = (int32_t)(__ldg(p.outer_off + (s2 >> p.n_in)) - block_off);
-                        e.J = t.J;
-                        e.ar = t.ar;
-                        e.ai = t.ai;
-                    }
-                }
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) s_out[base + __popc(m & ((1u << threadIdx.x) - 1u))] = e;
-            base += __popc(m);
-        }
-        if (threadIdx.x == 0) s_n = base;
-    }
-    __syncthreads();
-    const int nout = s_n;
+    if (STAGE || !UNIF) __syncthreads();
+    // this block's outer entries and straddling terms, listed per outer configuration
+    const uint32_t o0 = __ldg(p.optr + it.a), o1 = __ldg(p.optr + it.a + 1);
+    const uint32_t m0 = __ldg(p.mptr + it.a), m1 = __ldg(p.mptr + it.a + 1);
     const uint32_t rmask = (1u << p.rbits) - 1u;
     for (uint32_t r = threadIdx.x; r < it.count; r += blockDim.x) {
         const uint32_t row = (uint32_t)it.row0 + r;
@@ -350,8 +314,8 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
         const T2 xd = STAGE ? xs[r] : x[row];
         A accr = 0, acci = 0;
 #pragma unroll 2
-        for (int k = 0; k < nout; ++k) {
-            const OutEnt<A> e = s_out[k];
+        for (uint32_t k = o0; k < o1; ++k) {
+            const OutEnt<A> e = p.oent[k];
             const T2 xv = x[row + e.delta];
             A ar = e.ar, ai = e.ai;
             if (OJ && (__popc(s & e.J) & 1)) {
@@ -377,24 +341,25 @@ __global__ void __launch_bounds__(kBlock) spmv_fast_kernel(const FastParams<A> p
                 cmac<A>(accr, acci, ar, ai, xv, REAL);
             }
         }
-        for (int k = 0; k < p.n_mixed; ++k) {
-            const KTerm<uint32_t, A> t = mixed[k];
+        for (uint32_t j = m0; j < m1; ++j) {
+            const uint2 mk = __ldg(p.ment + j);
+            const KTerm<uint32_t, A> t = p.mixed[mk.x];
             if ((s & t.C) != t.V) continue;
             const uint32_t s2 = s ^ t.X;
             if ((t.flags & 1u) && !in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2))
                 continue;
             const uint32_t b2 = s2 & p.in_mask;
-            const uint32_t idx = __ldg(p.outer_off + (s2 >> p.n_in)) + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+            const uint32_t idx = mk.y + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
             A ar, ai;
             term_amp<uint32_t, A>(t, s, p.vars, ar, ai);
             cmac<A>(accr, acci, ar, ai, x[idx], REAL);
         }
         {
-            const A dr = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc] : __ldg(p.dtab + 2 * dc);
+            const A dr = __ldg(p.dtab + 2 * dc);
             accr = fma(dr, (A)xd.x, accr);
             acci = fma(dr, (A)xd.y, acci);
             if (!REAL) {
-                const A di = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc + 1] : __ldg(p.dtab + 2 * dc + 1);
+                const A di = __ldg(p.dtab + 2 * dc + 1);
                 accr = fma(-di, (A)xd.y, accr);
                 acci = fma(di, (A)xd.x, acci);
             }
@@ -467,18 +432,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         scale = sizeof(A) == 4 ? (A)o.scale32 : (A)o.scale;  // no per-thread FP64 conversion for FP32
         bprev = sizeof(A) == 4 ? (A)o.bprev32 : (A)o.bprev;
     }
-    __shared__ OutEnt<A> s_out[kMaxOuter];
     __shared__ A s_iamp[2 * kMaxInnerTable];
-    __shared__ KTerm<uint32_t, A> s_mixed[kMaxMixedSmem];
-    __shared__ A s_dtab[512];
-    __shared__ uint2 s_mx[kMaxMixedSmem];  // straddling terms possible in this block: (term, target block offset)
-    __shared__ int s_n, s_nmx;
-    const bool mixed_smem = p.n_mixed <= kMaxMixedSmem;
-    if (mixed_smem)
-        for (int t = threadIdx.x; t < p.n_mixed; t += blockDim.x) s_mixed[t] = p.mixed[t];
-    if (p.diag_mode == DIAG_U8)
-        for (int t = threadIdx.x; t < 2 * p.n_dtab; t += blockDim.x) s_dtab[t] = p.dtab[t];
-    const KTerm<uint32_t, A>* mixed = mixed_smem ? s_mixed : p.mixed;
     const WorkItem it = p.items[blockIdx.x];
     const uint32_t block_off = __ldg(p.outer_off + it.a);
     if (STAGE)  // the item is the whole outer block: rows [block_off, block_off + count)
@@ -492,56 +446,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
             s_iamp[2 * t + 1] = neg ? -k.ai : k.ai;
         }
     }
-    if (threadIdx.x < 32) {
-        const uint32_t b0 = p.inner_state ? __ldg(p.inner_state + it.inner_base) : it.inner_base;
-        const uint32_t s0 = (it.a << p.n_in) | b0;
-        int base = 0;
-        for (int t0 = 0; t0 < p.n_outer; t0 += 32) {
-            const int ti = t0 + (int)threadIdx.x;
-            bool ok = false;
-            OutEnt<A> e;
-            if (ti < p.n_outer) {
-                const KTerm<uint32_t, A> t = p.outer[ti];
-                if ((s0 & t.C) == t.V) {
-                    const uint32_t s2 = s0 ^ t.X;
-                    if (!(t.flags & 1u) || in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2)) {
-                        ok = true;
-                        e.delta = (int32_t)(__ldg(p.outer_off + (s2 >> p.n_in)) - block_off);
-                        e.J = t.J;
-                        e.ar = t.ar;
-                        e.ai = t.ai;
-                    }
-                }
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) s_out[base + __popc(m & ((1u << threadIdx.x) - 1u))] = e;
-            base += __popc(m);
-        }
-        if (threadIdx.x == 0) s_n = base;
-    } else if (threadIdx.x < 64 && mixed_smem) {
-        // straddling terms whose outer-bit condition holds in this block, with
-        // the offset of the (uniform) target block
-        const uint32_t lane = threadIdx.x - 32u, sa = it.a << p.n_in, omask = ~p.in_mask;
-        int base = 0;
-        for (int t0 = 0; t0 < p.n_mixed; t0 += 32) {
-            const int ti = t0 + (int)lane;
-            bool ok = false;
-            uint32_t boff = 0;
-            if (ti < p.n_mixed) {
-                const KTerm<uint32_t, A> t = p.mixed[ti];
-                if ((sa & t.C & omask) == (t.V & omask)) {
-                    ok = true;
-                    boff = __ldg(p.outer_off + ((sa ^ t.X) >> p.n_in));
-                }
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) s_mx[base + __popc(m & ((1u << lane) - 1u))] = make_uint2((uint32_t)ti, boff);
-            base += __popc(m);
-        }
-        if (lane == 0) s_nmx = base;
-    }
-    __syncthreads();
-    const int nout = s_n;
+    if (STAGE || !UNIF) __syncthreads();
+    // this block's outer entries and straddling terms (with their target block
+    // offsets), listed per outer configuration at construction
+    const uint32_t o0 = __ldg(p.optr + it.a), o1 = __ldg(p.optr + it.a + 1);
+    const uint32_t m0 = __ldg(p.mptr + it.a), m1 = __ldg(p.mptr + it.a + 1);
     const uint32_t rmask = (1u << p.rbits) - 1u;
 
     A dot_hi = 0, dot_lo = 0;
@@ -567,8 +476,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         ar_[q] = 0;
         ai_[q] = 0;
     }
-    for (int k = 0; k < nout; ++k) {
-        const OutEnt<A> e = s_out[k];
+    for (uint32_t k = o0; k < o1; ++k) {
+        const OutEnt<A> e = p.oent[k];
         T2 xv[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q)
@@ -656,12 +565,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         }
     }
 #endif
-    const int nmx = mixed_smem ? s_nmx : p.n_mixed;
-    for (int j = 0; j < nmx; ++j) {
+    for (uint32_t j = m0; j < m1; ++j) {
         // the four rows' targets first (their rank lookups in flight together),
         // then the gathers, then the sums
-        const uint2 mk = mixed_smem ? s_mx[j] : make_uint2((uint32_t)j, 0u);
-        const KTerm<uint32_t, A> t = mixed[mk.x];
+        const uint2 mk = __ldg(p.ment + j);
+        const KTerm<uint32_t, A> t = p.mixed[mk.x];
         uint32_t idx[RT];
         bool ok[RT];
 #pragma unroll
@@ -673,8 +581,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
             idx[q] = 0;
             if (ok[q]) {
                 const uint32_t b2 = s2 & p.in_mask;
-                const uint32_t boff = mixed_smem ? mk.y : __ldg(p.outer_off + (s2 >> p.n_in));
-                idx[q] = boff + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
+                idx[q] = mk.y + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
             }
         }
         T2 xv[RT];
@@ -703,11 +610,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
         if (!live[q]) continue;
-        const A dr = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc[q]] : __ldg(p.dtab + 2 * dc[q]);
+        const A dr = __ldg(p.dtab + 2 * dc[q]);
         A accr = fma(dr, (A)xd[q].x, ar_[q]);
         A acci = fma(dr, (A)xd[q].y, ai_[q]);
         if (!REAL) {
-            const A di = p.diag_mode == DIAG_U8 ? s_dtab[2 * dc[q] + 1] : __ldg(p.dtab + 2 * dc[q] + 1);
+            const A di = __ldg(p.dtab + 2 * dc[q] + 1);
             accr = fma(-di, (A)xd[q].y, accr);
             acci = fma(di, (A)xd[q].x, acci);
         }
@@ -1041,6 +948,41 @@ void Hamiltonian::build_fast() {
     }
     u_ar_ = amp0.real();
     u_ai_ = amp0.imag();
+    // Per outer configuration a (every row of block a shares its outer bits):
+    // the outer terms whose condition holds, with the offset of their target
+    // block, and the straddling terms whose outer-bit condition holds, with
+    // their (uniform) target block.  Built once here instead of by every CTA.
+    const uint64_t n_a = 1ull << B.n_out;
+    std::vector<uint32_t> optr(n_a + 1, 0), mptr(n_a + 1, 0);
+    std::vector<std::pair<uint32_t, int32_t>> oraw;  // (outer term, delta)
+    std::vector<uint2> ment;
+    for (uint64_t a = 0; a < n_a; ++a) {
+        optr[a] = (uint32_t)oraw.size();
+        mptr[a] = (uint32_t)ment.size();
+        if (B.outer_off[a + 1] == B.outer_off[a]) continue;
+        const int c = B.inner_class_of((uint32_t)a);
+        const uint64_t b0 = B.inner_all ? 0 : B.inner_state[B.class_base[c]];
+        const uint64_t s0 = (a << B.n_in) | b0;
+        for (size_t t = 0; t < outer.size(); ++t) {
+            const HostTerm& h = *outer[t];
+            if ((s0 & h.C) != h.V) continue;
+            const uint64_t s2 = s0 ^ h.X;
+            if (h.check && !B.contains_int(s2)) continue;
+            oraw.push_back({(uint32_t)t, (int32_t)((int64_t)B.outer_off[s2 >> B.n_in] - (int64_t)B.outer_off[a])});
+        }
+        const uint64_t sa = a << B.n_in;
+        for (size_t t = 0; t < mixed.size(); ++t) {
+            const HostTerm& h = *mixed[t];
+            if ((sa & h.C & ~inm) != (h.V & ~inm)) continue;
+            ment.push_back(make_uint2((uint32_t)t, (uint32_t)B.outer_off[(sa ^ h.X) >> B.n_in]));
+        }
+        if (oraw.size() > 0xFFFFFFF0ull || ment.size() > 0xFFFFFFF0ull) return;
+    }
+    optr[n_a] = (uint32_t)oraw.size();
+    mptr[n_a] = (uint32_t)ment.size();
+    upload_vec(optr_, optr);
+    upload_vec(mptr_, mptr);
+    upload_vec(ment_, ment);
     auto build = [&](auto tag, FastSet& fs) {
         using A = decltype(tag);
         std::vector<KTerm<uint32_t, A>> ko, ki, km;
@@ -1048,6 +990,15 @@ void Hamiltonian::build_fast() {
         pack<uint32_t, A>(outer, ko, dummy);
         pack<uint32_t, A>(inner, ki, dummy);
         pack<uint32_t, A>(mixed, km, vars);
+        std::vector<OutEnt<A>> oe(oraw.size());
+        for (size_t i = 0; i < oraw.size(); ++i) {
+            const KTerm<uint32_t, A>& k = ko[oraw[i].first];
+            oe[i].delta = oraw[i].second;
+            oe[i].J = k.J;
+            oe[i].ar = k.ar;
+            oe[i].ai = k.ai;
+        }
+        upload_vec(fs.oent, oe);
         upload_vec(fs.outer, ko);
         upload_vec(fs.inner, ki);
         upload_vec(fs.mixed, km);
@@ -1227,6 +1178,10 @@ void Hamiltonian::fast_params(FastParams<A>& p) const {
     p.mixed = fs.mixed.as<KTerm<uint32_t, A>>();
     p.vars = fs.vars.as<KVar<A>>();
     p.n_mixed = fs.n_mixed;
+    p.optr = optr_.as<uint32_t>();
+    p.oent = fs.oent.as<OutEnt<A>>();
+    p.mptr = mptr_.as<uint32_t>();
+    p.ment = ment_.as<uint2>();
     p.diag_mode = diag_mode_;
     const DBuf& dtab = sizeof(A) == 8 ? dtab64_ : dtab32_;
     p.n_dtab = (int)(dtab.bytes / (2 * sizeof(A)));
