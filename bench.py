@@ -394,6 +394,13 @@ def cf_batch(qk, hbm_peak, peak_kind):
             ops.add_term(ph[j], "Sz", j)
         phis.append(qk.MatrixFreeHamiltonian(b, qk.SpinHalfSite(), ops).apply(psi))
     t_rhs = time.perf_counter() - t0
+    # the right-hand sides in pinned host memory, as the e2e rule has it
+    nbytes = len(phis) * H.dimension * 16
+    P = np.frombuffer((ctypes.c_char * nbytes).from_address(_pinned(_cudart(), nbytes)), dtype=np.complex128)
+    P = P.reshape(len(phis), H.dimension)
+    for i, ph in enumerate(phis):
+        P[i] = ph
+    phis = P
     omegas = np.linspace(0.0, 4.0, CF_NOMEGA)
     out = {}
     for mixed in (True, False):

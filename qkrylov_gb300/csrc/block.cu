@@ -473,10 +473,14 @@ public:
         if (!items.empty()) QKG_CUDA(cudaMemcpy(items_.p, items.data(), items.size() * sizeof(BItem), cudaMemcpyHostToDevice));
         range_.alloc(range.size() * sizeof(uint32_t));
         QKG_CUDA(cudaMemcpy(range_.p, range.data(), range.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-        const size_t vbytes = std::max<uint64_t>(1, rows_) * Rp * sizeof(T2);
-        for (auto& b : buf_) {
-            b.alloc(vbytes);
-            QKG_CUDA(cudaMemsetAsync(b.p, 0, vbytes, s_));
+        // the three rotating block vectors live in the first Hamiltonian's
+        // Krylov workspace, kept between calls (freeing 13 GB costs milliseconds
+        // and fresh pages slow the first steps)
+        const size_t vbytes = (std::max<uint64_t>(1, rows_) * Rp * sizeof(T2) + 255) / 256 * 256;
+        char* ws = static_cast<char*>(hs[0]->krylov_workspace(3 * vbytes).p);
+        for (int i = 0; i < 3; ++i) {
+            buf_[i] = ws + (size_t)i * vbytes;
+            QKG_CUDA(cudaMemsetAsync(buf_[i], 0, vbytes, s_));
         }
         apart_.alloc(std::max<size_t>(1, n_items_) * Rp * sizeof(double));
         bpart_.alloc(std::max<size_t>(1, n_items_) * Rp * sizeof(double));
@@ -484,7 +488,7 @@ public:
 
     uint64_t rows() const { return rows_; }
     size_t n_items() const { return n_items_; }
-    T2* buf(int i) { return buf_[i].template as<T2>(); }
+    T2* buf(int i) { return static_cast<T2*>(buf_[i]); }
 
     void spmv(int vpl, const T2* x, T2* y, const double* scale, double* apart) {
         const auto* P = params_.as<FastParams<A>>();
@@ -565,7 +569,7 @@ private:
     size_t n_items_ = 0;
     std::vector<uint64_t> dims_, bases_;
     DBuf params_, items_, range_, apart_, bpart_;
-    DBuf buf_[3];
+    void* buf_[3] = {nullptr, nullptr, nullptr};
 
 public:
     double* apart() { return apart_.as<double>(); }
@@ -764,9 +768,11 @@ BlockTridiag block_lanczos(const std::vector<Hamiltonian*>& hs, const BlockOpts&
 void ftlm_observables_block(const BlockTridiag& t, const double* betas, int nb, double* Zo, double* Eo, double* Co,
                             bool shifted, double* log_zmax) {
     // per vector: eigenvalues and squared first components (ftlm.cpp:61-119)
-    std::vector<FTLMTri> tri;
-    for (size_t v = 0; v < t.alpha.size(); ++v) {
-        FTLMTri x;
+    // (independent per vector: spread over the host cores)
+    std::vector<FTLMTri> tri(t.alpha.size());
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long v = 0; v < (long long)t.alpha.size(); ++v) {
+        FTLMTri& x = tri[v];
         x.norm2 = t.norm2[v];
         const auto& a = t.alpha[v];
         if (!a.empty()) {
@@ -777,7 +783,6 @@ void ftlm_observables_block(const BlockTridiag& t, const double* betas, int nb, 
             x.w0.resize(x.evals.size());
             for (size_t j = 0; j < x.evals.size(); ++j) x.w0[j] = z[j] * z[j];
         }
-        tri.push_back(std::move(x));
     }
     // Z_h carries 1/R (ftlm.cpp:160-162): the sum over Hamiltonians of the
     // per-Hamiltonian estimates is the plain sum over all vectors divided by R.

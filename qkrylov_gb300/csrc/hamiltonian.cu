@@ -1344,7 +1344,10 @@ void Hamiltonian::build_diagonal() {
         const size_t take = (size_t)std::min<unsigned long long>(nm, cap);
         hmiss.resize(take);
         QKG_CUDA(cudaMemcpy(hmiss.data(), missing.p, take * sizeof(ulonglong2), cudaMemcpyDeviceToHost));
-        for (const auto& m : hmiss) table.insert({m.x, m.y});
+        for (const auto& m : hmiss) {
+            table.insert({m.x, m.y});
+            if (table.size() > 65536) break;  // too many values for codes: stop inserting
+        }
         if (table.size() > 65536) { full = true; break; }
     }
     if (!n) { diag_mode_ = DIAG_U8; table.insert({0, 0}); }
