@@ -356,9 +356,28 @@ class MatrixFreeHamiltonian(_Handle):
         return int(lib().qkrylov_hamiltonian_dimension(self._h))
 
     def apply(self, x):
+        """y = H x.  Host arrays (NumPy, complex128) go through host memory;
+        a CUDA tensor (torch, complex128 or complex64, contiguous, on this
+        device) is applied in place on the device without host copies, on the
+        tensor's current stream, and a tensor of the same type is returned."""
+        if hasattr(x, "__cuda_array_interface__"):
+            return self._apply_cuda(x)
         x = _cvec(x, self.dimension)
         y = _np.empty_like(x)
         _check(lib().qkrylov_hamiltonian_apply_complex_f64(self._h, _dptr(x.view(_np.float64)), _dptr(y.view(_np.float64))))
+        return y
+
+    def _apply_cuda(self, x):
+        import torch
+        if not isinstance(x, torch.Tensor):
+            raise TypeError("device arrays other than torch tensors: use apply_device with raw pointers")
+        if x.dtype not in (torch.complex128, torch.complex64):
+            raise TypeError("device vectors must be complex128 or complex64")
+        if x.dim() != 1 or x.numel() != self.dimension or not x.is_contiguous():
+            raise ValueError(f"expected a contiguous vector of length {self.dimension}")
+        y = torch.empty_like(x)
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        self.apply_device(x.data_ptr(), y.data_ptr(), stream=stream, fp32=x.dtype == torch.complex64)
         return y
 
     __matmul__ = apply

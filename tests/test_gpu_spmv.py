@@ -164,6 +164,27 @@ def test_edge_cases(qk):
         H.apply(np.zeros(3, dtype=complex))
 
 
+@pytest.mark.parametrize("m", [M.heisenberg(16, True, 0), M.hubbard(6, True, 3, 2)])
+def test_apply_torch_cuda_tensor_zero_copy(qk, m):
+    """H.apply on a torch CUDA tensor (complex128 and complex64) runs on the
+    device pointers in reference order and matches the host path."""
+    torch = pytest.importorskip("torch")
+    b, s, o = make_model(qk, *m)
+    H = qk.MatrixFreeHamiltonian(b, s, o)
+    rng = np.random.default_rng(4)
+    x = rng.normal(size=H.dimension) + 1j * rng.normal(size=H.dimension)
+    y = H.apply(x)
+    xt = torch.from_numpy(x).to("cuda:0")
+    yt = H.apply(xt)
+    assert isinstance(yt, torch.Tensor) and yt.is_cuda and yt.dtype == torch.complex128
+    np.testing.assert_allclose(yt.cpu().numpy(), y, rtol=0, atol=RTOL64 * np.abs(y).max())
+    y32 = H.apply(xt.to(torch.complex64))
+    assert y32.dtype == torch.complex64
+    np.testing.assert_allclose(y32.cpu().numpy(), y, rtol=0, atol=RTOL32 * np.abs(y).max() * 4)
+    with pytest.raises(ValueError):
+        H.apply(xt[:-1])
+
+
 def test_reference_c_api_float_entry_points(qk):
     """tests/test_c_api.cpp:92-149 through the float ABI."""
     L = qk.lib()
