@@ -16,8 +16,33 @@ namespace {
 using clk = std::chrono::steady_clock;
 inline double secs(clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); }
 
+// Device vectors of one size recycled within a solve: a Davidson iteration
+// otherwise allocates and frees gigabytes (corrections, restarts), and both
+// cudaFree and the first touch of fresh pages cost milliseconds per GB.
+struct VecPool {
+    size_t bytes;
+    std::vector<DBuf> free;
+    explicit VecPool(size_t b) : bytes(b) {}
+    DBuf get(size_t held) {
+        if (!free.empty()) {
+            DBuf b = std::move(free.back());
+            free.pop_back();
+            return b;
+        }
+        size_t fr = 0, tot = 0;
+        QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+        if (fr < bytes + (64ull << 20))
+            throw Error(CUDA_ERR, "out of device memory for the Krylov basis (" + std::to_string(held) + " vectors held)");
+        return DBuf(bytes);
+    }
+    void put(DBuf&& b) {
+        if (b.p) free.push_back(std::move(b));
+    }
+};
+
 // A growing list of device vectors plus the device array of their pointers
-// (what the multi-vector kernels take).
+// (what the multi-vector kernels take); with a pool, vectors come from and go
+// back to it.
 template <class T2>
 struct VecList {
     uint64_t n = 0;
@@ -25,13 +50,26 @@ struct VecList {
     std::vector<T2*> host_ptrs;
     DBuf dev_ptrs;
     size_t cap = 0;
-    explicit VecList(uint64_t n_) : n(n_) {}
+    VecPool* pool = nullptr;
+    explicit VecList(uint64_t n_, VecPool* p = nullptr) : n(n_), pool(p) {}
+    ~VecList() { clear(); }
     T2* push() {
-        size_t fr = 0, tot = 0;
-        QKG_CUDA(cudaMemGetInfo(&fr, &tot));
-        if (fr < n * sizeof(T2) + (64ull << 20))
-            throw Error(CUDA_ERR, "out of device memory for the Krylov basis (" + std::to_string(bufs.size()) + " vectors held)");
-        bufs.emplace_back(n * sizeof(T2));
+        if (pool) {
+            bufs.push_back(pool->get(bufs.size()));
+        } else {
+            size_t fr = 0, tot = 0;
+            QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+            if (fr < n * sizeof(T2) + (64ull << 20))
+                throw Error(CUDA_ERR, "out of device memory for the Krylov basis (" + std::to_string(bufs.size()) + " vectors held)");
+            bufs.emplace_back(n * sizeof(T2));
+        }
+        host_ptrs.push_back(bufs.back().as<T2>());
+        sync_ptrs();
+        return host_ptrs.back();
+    }
+    // append a vector that is already on the device (n elements), taking ownership
+    T2* adopt(DBuf&& b) {
+        bufs.push_back(std::move(b));
         host_ptrs.push_back(bufs.back().as<T2>());
         sync_ptrs();
         return host_ptrs.back();
@@ -44,8 +82,14 @@ struct VecList {
         if (!host_ptrs.empty())
             QKG_CUDA(cudaMemcpy(dev_ptrs.p, host_ptrs.data(), host_ptrs.size() * sizeof(T2*), cudaMemcpyHostToDevice));
     }
-    void clear() { bufs.clear(); host_ptrs.clear(); }
+    void clear() {
+        if (pool)
+            for (auto& b : bufs) pool->put(std::move(b));
+        bufs.clear();
+        host_ptrs.clear();
+    }
     void take(std::vector<DBuf>& nb) {
+        clear();
         bufs = std::move(nb);
         host_ptrs.clear();
         for (auto& b : bufs) host_ptrs.push_back(b.as<T2>());
@@ -693,7 +737,8 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
     std::mt19937 rng(1234);
     std::uniform_real_distribution<double> dist(-1.0, 1.0);
     std::uniform_real_distribution<float> dist32(-1.0f, 1.0f);
-    VecList<T2> V(n), HV(n);
+    VecPool pool(n * sizeof(T2));  // declared before the lists, so it outlives them
+    VecList<T2> V(n, &pool), HV(n, &pool);
     std::vector<cd> hv(n), c;
     const int passes = MIXED ? 2 : 1;
     auto orthonormalize = [&](T2* t) -> double {
@@ -769,7 +814,7 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
             out.residuals[k] = rn;
             if (rn > tol) {
                 all_conv = false;
-                DBuf t(n * sizeof(T2));
+                DBuf t = pool.get(V.size() + HV.size());
                 Op::precond(rptr[k], diag.as<double2>(), ev[k], t.as<T2>(), n, st);
                 corr.push_back(std::move(t));
             }
@@ -825,8 +870,8 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
             std::vector<DBuf> nv, nh;
             std::vector<T2*> pv, ph;
             for (int k = 0; k < n_eig; ++k) {
-                nv.emplace_back(n * sizeof(T2));
-                nh.emplace_back(n * sizeof(T2));
+                nv.push_back(pool.get(V.size() + HV.size()));
+                nh.push_back(pool.get(V.size() + HV.size()));
                 pv.push_back(nv.back().as<T2>());
                 ph.push_back(nh.back().as<T2>());
             }
@@ -846,11 +891,11 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
             const double nrm = orthonormalize(t.as<T2>());
             if (nrm > 1e-10) {
                 Op::scal(1.0 / nrm, t.as<T2>(), n, st);
-                T2* v = V.push();
-                QKG_CUDA(cudaMemcpyAsync(v, t.p, n * sizeof(T2), cudaMemcpyDeviceToDevice, st));
+                T2* v = V.adopt(std::move(t));
                 Op::apply(H, v, HV.push(), st);
             }
         }
+        for (auto& t : corr) pool.put(std::move(t));  // the rejected ones
     }
     return out;
 }
