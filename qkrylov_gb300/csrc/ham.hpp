@@ -226,6 +226,10 @@ void mdot_f64(const double2* const* V_dev, int k, const double2* w, uint64_t n, 
               Workspace& ws, cudaStream_t s);
 void mdot_f32(const float2* const* V_dev, int k, const float2* w, uint64_t n, std::complex<double>* out,
               Workspace& ws, cudaStream_t s);
+// out[o * k + j] = <V_j, W_o> for j < k, o < nw <= 4: one pass over the V_j for
+// all W_o (compensated FP32; W a host array of device pointers).
+void mdot_multi_f32(const float2* const* V_dev, int k, float2* const* W, int nw, uint64_t n,
+                    std::complex<double>* out, Workspace& ws, cudaStream_t s);
 // w += sum_j c[j] V_j  (c given on the host, k <= 1024)
 void mcombine_f64(const double2* const* V_dev, int k, const std::complex<double>* c, double2* w, uint64_t n,
                   Workspace& ws, cudaStream_t s);

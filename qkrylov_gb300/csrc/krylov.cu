@@ -43,6 +43,44 @@ __device__ __forceinline__ void ff_add_prod(FF& acc, float a, float b) {
     acc.lo += err + e;
 }
 __device__ __forceinline__ double ff_value(const FF& a) { return (double)a.hi + (double)a.lo; }
+// a += b in float-float arithmetic
+__device__ __forceinline__ void ff_add_ff(FF& a, FF b) {
+    const float t = a.hi + b.hi;
+    const float z = t - a.hi;
+    a.lo += ((a.hi - (t - z)) + (b.hi - z)) + b.lo;
+    a.hi = t;
+}
+// Block sum of a complex float-float value, all in FP32 arithmetic (GB300's
+// FP64 pipe is narrow: a double reduction per output and CTA costs more than
+// the pass it finishes); thread 0 writes the result, rounded to double, to *dst.
+__device__ __forceinline__ void block_sum_cff(FF re, FF im, double2* dst) {
+    __shared__ FF sre[32], sim[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        FF r2{__shfl_down_sync(0xffffffffu, re.hi, o), __shfl_down_sync(0xffffffffu, re.lo, o)};
+        FF i2{__shfl_down_sync(0xffffffffu, im.hi, o), __shfl_down_sync(0xffffffffu, im.lo, o)};
+        ff_add_ff(re, r2);
+        ff_add_ff(im, i2);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();  // the arrays may still be read from the previous call
+    if (lane == 0) {
+        sre[wid] = re;
+        sim[wid] = im;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const bool on = threadIdx.x < (blockDim.x >> 5);
+        re = on ? sre[lane] : FF{0.f, 0.f};
+        im = on ? sim[lane] : FF{0.f, 0.f};
+        for (int o = 16; o > 0; o >>= 1) {
+            FF r2{__shfl_down_sync(0xffffffffu, re.hi, o), __shfl_down_sync(0xffffffffu, re.lo, o)};
+            FF i2{__shfl_down_sync(0xffffffffu, im.hi, o), __shfl_down_sync(0xffffffffu, im.lo, o)};
+            ff_add_ff(re, r2);
+            ff_add_ff(im, i2);
+        }
+    }
+    if (threadIdx.x == 0) *dst = make_double2(ff_value(re), ff_value(im));
+}
 
 // ---- block reduction of double pairs ---------------------------------------
 __device__ __forceinline__ double2 warp_sum(double2 v) {
@@ -306,11 +344,76 @@ __global__ void __launch_bounds__(kThreads) mdot32_kernel(const float2* const* _
     }
 #pragma unroll
     for (int q = 0; q < KB32; ++q) {
-        if (q < kk) {
-            const double2 s = block_sum(make_double2(ff_value(re[q]), ff_value(im[q])));
-            if (threadIdx.x == 0) part[(size_t)(j0 + q) * stride + blockIdx.x] = s;
-        }
+        if (q < kk) block_sum_cff(re[q], im[q], part + (size_t)(j0 + q) * stride + blockIdx.x);
     }
+}
+
+// FP32 projections <V_j, W_o> (compensated) for a column of up to KBM vectors
+// V_j and NW vectors W_o: every V_j is read once and every W_o once per
+// column, where NW separate projections would read every V_j NW times.
+constexpr int KBM = 4;
+template <int NW>
+__global__ void __launch_bounds__(kThreads) mdot32_multi_kernel(const float2* const* __restrict__ V, int k,
+                                                                const float2* const* __restrict__ W, uint64_t n,
+                                                                double2* part, int stride) {
+    const int j0 = blockIdx.y * KBM;
+    const int kk = min(KBM, k - j0);
+    FF re[KBM][NW], im[KBM][NW];
+    const float2* vp[KBM];
+    const float2* wp[NW];
+    bool al = true;
+#pragma unroll
+    for (int q = 0; q < KBM; ++q) {
+        vp[q] = V[j0 + (q < kk ? q : 0)];
+        al = al && (reinterpret_cast<uintptr_t>(vp[q]) & 15u) == 0;
+#pragma unroll
+        for (int o = 0; o < NW; ++o) re[q][o] = im[q][o] = FF{0.f, 0.f};
+    }
+#pragma unroll
+    for (int o = 0; o < NW; ++o) {
+        wp[o] = W[o];
+        al = al && (reinterpret_cast<uintptr_t>(wp[o]) & 15u) == 0;
+    }
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    uint64_t done = 0;
+    if (al) {
+        const uint64_t n2 = n / 2;
+        for (uint64_t i = t0; i < n2; i += step) {
+            float4 b[NW];
+#pragma unroll
+            for (int o = 0; o < NW; ++o) b[o] = reinterpret_cast<const float4*>(wp[o])[i];
+#pragma unroll
+            for (int q = 0; q < KBM; ++q) {
+                if (q < kk) {
+                    const float4 a = reinterpret_cast<const float4*>(vp[q])[i];
+#pragma unroll
+                    for (int o = 0; o < NW; ++o) {
+                        ff_cmac(re[q][o], im[q][o], a.x, a.y, b[o].x, b[o].y);
+                        ff_cmac(re[q][o], im[q][o], a.z, a.w, b[o].z, b[o].w);
+                    }
+                }
+            }
+        }
+        done = 2 * n2;
+    }
+    for (uint64_t i = done + t0; i < n; i += step) {
+#pragma unroll
+        for (int q = 0; q < KBM; ++q)
+            if (q < kk) {
+                const float2 a = vp[q][i];
+#pragma unroll
+                for (int o = 0; o < NW; ++o) {
+                    const float2 b = wp[o][i];
+                    ff_cmac(re[q][o], im[q][o], a.x, a.y, b.x, b.y);
+                }
+            }
+    }
+#pragma unroll
+    for (int q = 0; q < KBM; ++q)
+#pragma unroll
+        for (int o = 0; o < NW; ++o)
+            if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.x);
 }
 
 // w += sum_j c_j V_j ; coefficients (complex double) in global memory.
@@ -527,6 +630,29 @@ void mdot_f64(const double2* const* V, int k, const double2* w, uint64_t n, std:
 void mdot_f32(const float2* const* V, int k, const float2* w, uint64_t n, std::complex<double>* out, Workspace& ws,
               cudaStream_t s) {
     mdot_impl<float2, true>(V, k, w, n, out, ws, s);
+}
+void mdot_multi_f32(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,
+                    Workspace& ws, cudaStream_t s) {
+    if (k <= 0 || nw <= 0) return;
+    QKG_REQUIRE(nw <= 4 && (size_t)k * nw <= 4088, "mdot_multi: at most 4 right-hand vectors and 4088 products");
+    // the W pointer table goes through the result slots (read by the kernel before finish overwrites them)
+    float2** dw = reinterpret_cast<float2**>(ws.result.as<double2>() + 4096 - 8);
+    QKG_CUDA(cudaMemcpyAsync(dw, W, (size_t)nw * sizeof(float2*), cudaMemcpyHostToDevice, s));
+    int g = stream_grid(n);
+    g = (int)std::min<size_t>((size_t)g, ws.cap_partials / ((size_t)k * nw));
+    g = std::max(1, g);
+    const dim3 grid(g, (k + KBM - 1) / KBM);
+    double2* part = ws.partial.as<double2>();
+    switch (nw) {
+        case 1: mdot32_multi_kernel<1><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        case 2: mdot32_multi_kernel<2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        case 3: mdot32_multi_kernel<3><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        default: mdot32_multi_kernel<4><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+    }
+    QKG_LAUNCHED();
+    const double2* r = finish(ws, g, g, k * nw, s);
+    for (int j = 0; j < k; ++j)
+        for (int o = 0; o < nw; ++o) out[(size_t)o * k + j] = {r[(size_t)j * nw + o].x, r[(size_t)j * nw + o].y};
 }
 
 template <class T2, class A>

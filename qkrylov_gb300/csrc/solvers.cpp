@@ -691,9 +691,21 @@ template <> struct DavOps<float2> {
     static void precond(const float2* r, const double2* d, double l, float2* t, uint64_t n, cudaStream_t s) {
         davidson_precond_f32(r, d, l, t, n, s);
     }
+    static void mdot_multi(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, cd* o, Workspace& ws,
+                           cudaStream_t s) {
+        mdot_multi_f32(V, k, W, nw, n, o, ws, s);
+    }
     static void from64(const double2* x, float2* y, uint64_t n, cudaStream_t s) { f64_to_f32(x, y, n, s); }
     static void to64(const float2* x, double2* y, uint64_t n, cudaStream_t s) { f32_to_f64(x, y, n, s); }
 };
+
+inline void mdot_block(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, cd* o, Workspace& ws,
+                       cudaStream_t s) {
+    mdot_multi_f32(V, k, W, nw, n, o, ws, s);
+}
+inline void mdot_block(const double2* const*, int, double2* const*, int, uint64_t, cd*, Workspace&, cudaStream_t) {
+    QKG_REQUIRE(false, "block projection is used by the mixed form only");
+}
 
 // src/solvers/davidson.cpp:86-227 with the Krylov vectors stored in T2.
 // Projections <V_i, HV_j> of vectors that did not change are kept from the
@@ -715,7 +727,7 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
     n_eig = (int)std::min<uint64_t>((uint64_t)n_eig, n);
     max_sub = std::max(max_sub, 2 * n_eig);
     QKG_REQUIRE(max_sub + n_eig <= 1024, "Davidson: subspace limited to 1024 vectors");
-    Workspace ws(ws_cap(max_sub + n_eig + 2));
+    Workspace ws(ws_cap(4 * (max_sub + n_eig + 2)));  // block projections: 4 right-hand vectors
     DBuf diag(n * sizeof(double2)), tmp, d64(n * sizeof(double2));
     H.diagonal_f64(diag.as<double2>(), st);
     // Seeds: unit vectors at the n_eig smallest diagonal entries, in the order
@@ -741,12 +753,14 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
     VecList<T2> V(n, &pool), HV(n, &pool);
     std::vector<cd> hv(n), c;
     const int passes = MIXED ? 2 : 1;
-    auto orthonormalize = [&](T2* t) -> double {
-        for (int p = 0; p < passes && V.size(); ++p) {
-            c.assign(V.size(), 0.0);
-            Op::mdot(V.dev(), (int)V.size(), t, n, c.data(), ws, st);
+    // t -= V[from..] (V[from..]^H t), passes times, and ||t||
+    auto orthonormalize = [&](T2* t, size_t from) -> double {
+        const int kv = (int)(V.size() - std::min(from, V.size()));
+        for (int p = 0; p < passes && kv; ++p) {
+            c.assign(kv, 0.0);
+            Op::mdot(V.dev() + from, kv, t, n, c.data(), ws, st);
             for (auto& x : c) x = -x;
-            Op::mcomb(V.dev(), (int)V.size(), c.data(), t, n, ws, st);
+            Op::mcomb(V.dev() + from, kv, c.data(), t, n, ws, st);
         }
         return std::sqrt(Op::nrm2sq(t, n, ws, st));
     };
@@ -756,13 +770,13 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
         hv[di[i]] = 1.0;
         upload_ref_f64(H, hv.data(), d64.as<double2>(), tmp);
         Op::from64(d64.as<double2>(), seed.as<T2>(), n, st);
-        double nrm = orthonormalize(seed.as<T2>());
+        double nrm = orthonormalize(seed.as<T2>(), 0);
         if (nrm < 1e-10) {
             if (f32_stream) fill_stream(rng, dist32, n, hv.data());
             else fill_stream(rng, dist, n, hv.data());
             upload_ref_f64(H, hv.data(), d64.as<double2>(), tmp);
             Op::from64(d64.as<double2>(), seed.as<T2>(), n, st);
-            nrm = orthonormalize(seed.as<T2>());
+            nrm = orthonormalize(seed.as<T2>(), 0);
         }
         T2* v = V.push();
         QKG_CUDA(cudaMemcpyAsync(v, seed.p, n * sizeof(T2), cudaMemcpyDeviceToDevice, st));
@@ -887,8 +901,30 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
             HV.take(nh);
             rows.clear();
         }
-        for (auto& t : corr) {  // orthogonalise each correction and extend (:213-223)
-            const double nrm = orthonormalize(t.as<T2>());
+        // Orthogonalise each correction and extend (:213-223).  Mixed form: all
+        // corrections are first projected off the current basis together (one
+        // pass over V per Gram-Schmidt pass for all of them), then each off the
+        // corrections accepted before it; in exact arithmetic the same as the
+        // sequential projection off the growing basis.
+        size_t from = 0;
+        if (MIXED && corr.size() > 1 && V.size()) {
+            const int kv = (int)V.size(), nc = (int)corr.size();
+            std::vector<T2*> tp;
+            for (auto& t : corr) tp.push_back(t.as<T2>());
+            const int wmax = std::max(1, std::min(4, 1024 / kv));  // coefficient table limit of mmulti
+            for (int c0 = 0; c0 < nc; c0 += wmax) {
+                const int nw = std::min(wmax, nc - c0);
+                std::vector<cd> cc((size_t)nw * kv);
+                for (int p = 0; p < passes; ++p) {
+                    mdot_block(V.dev(), kv, tp.data() + c0, nw, n, cc.data(), ws, st);
+                    for (auto& x : cc) x = -x;
+                    Op::mmulti(V.dev(), kv, cc.data(), tp.data() + c0, nw, n, true, ws, st);
+                }
+            }
+            from = V.size();
+        }
+        for (auto& t : corr) {
+            const double nrm = orthonormalize(t.as<T2>(), from);
             if (nrm > 1e-10) {
                 Op::scal(1.0 / nrm, t.as<T2>(), n, st);
                 T2* v = V.adopt(std::move(t));

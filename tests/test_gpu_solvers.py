@@ -196,8 +196,8 @@ def test_lanczos_from_given_start_matches_oracle(qk, oracle):
     assert abs(abs(np.vdot(r.eigenvector, evec)) - 1) < 1e-8
 
 
-@pytest.mark.parametrize("model", ["heis", "hub"])
-def test_davidson_mixed_vs_fp64(qk, model):
+@pytest.mark.parametrize("model,k", [("heis", 2), ("hub", 2), ("heis", 4)])
+def test_davidson_mixed_vs_fp64(qk, model, k):
     # mixed form: FP32 vectors and SpMV, FP64-accurate projections, FP64-refined
     # Ritz pairs; its eigenvalues agree with the FP64 form's to well below the
     # FP32 residual (error ~ residual^2 / gap)
@@ -206,9 +206,10 @@ def test_davidson_mixed_vs_fp64(qk, model):
     else:
         b, s, o = make_model(qk, M.HUBBARD, 6, M.sector(nup=3, ndn=2), M.hubbard_terms(6, False, U=3.0))
     H = qk.MatrixFreeHamiltonian(b, s, o)
-    r64 = qk.davidson_lowest_ex(H, n_eig=2, max_subspace=24, tol=1e-8, mixed=False)
+    # (k = 4: the mixed form projects four corrections per pass off the basis)
+    r64 = qk.davidson_lowest_ex(H, n_eig=k, max_subspace=24, tol=1e-8, mixed=False)
     assert r64.converged and np.all(r64.residuals <= 1e-8)
-    r32 = qk.davidson_lowest_ex(H, n_eig=2, max_subspace=24, tol=1e-5, mixed=True, return_vectors=True)
+    r32 = qk.davidson_lowest_ex(H, n_eig=k, max_subspace=24, tol=1e-5, mixed=True, return_vectors=True)
     assert r32.converged, r32.residuals
     assert np.all(r32.residuals <= 1e-5)
     np.testing.assert_allclose(r32.eigenvalues, r64.eigenvalues, rtol=0, atol=1e-8)
