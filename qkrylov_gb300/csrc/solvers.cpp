@@ -792,6 +792,21 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
     for (auto& r : rbuf) rptr.push_back(r.as<T2>());
     for (int iter = 0; iter < max_iter; ++iter) {
         const int m = (int)V.size();
+        if (MIXED && m - (int)rows.size() > 1) {
+            // the new rows together: one pass over HV_0..HV_{m-1} for up to four new V_i
+            for (int i0 = (int)rows.size(); i0 < m; i0 += 4) {
+                const int nw = std::min(4, m - i0);
+                std::vector<T2*> wp;
+                for (int o = 0; o < nw; ++o) wp.push_back(V[i0 + o]);
+                std::vector<cd> cc((size_t)nw * m);
+                mdot_block(HV.dev(), m, wp.data(), nw, n, cc.data(), ws, st);  // <HV_j, V_{i0+o}>
+                for (int o = 0; o < nw; ++o) {
+                    std::vector<cd> col(i0 + o + 1);
+                    for (int j = 0; j <= i0 + o; ++j) col[j] = std::conj(cc[(size_t)o * m + j]);
+                    rows.push_back(std::move(col));
+                }
+            }
+        }
         for (int i = (int)rows.size(); i < m; ++i) {
             std::vector<cd> col(i + 1);
             Op::mdot(HV.dev(), i + 1, V[i], n, col.data(), ws, st);  // <HV_j, V_i>
