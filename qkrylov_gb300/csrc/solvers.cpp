@@ -232,7 +232,82 @@ void tridiag_eig(const double* a, const double* b, int n, std::vector<double>& d
     }
 }
 
+// Lowest eigenpair of the symmetric tridiagonal (a, b) in O(n): the eigenvalue
+// by Sturm bisection (tridiag_lowest), the eigenvector by inverse iteration on
+// T - lambda I with a tridiagonal LU with row interchanges (Gaussian
+// elimination with partial pivoting; zero pivots replaced by eps ||T||).  The
+// QL algorithm with all eigenvector rows costs O(n^3): 13 ms at n = 200.
 double tridiag_ground(const double* a, const double* b, int n, std::vector<double>& vec) {
+    if (n <= 0) { vec.clear(); return 0.0; }
+    if (n == 1) { vec.assign(1, 1.0); return a[0]; }
+    const double lam = tridiag_lowest(a, b, n);
+    double tn = 0.0;
+    for (int i = 0; i < n; ++i)
+        tn = std::max(tn, std::abs(a[i]) + (i > 0 ? std::abs(b[i - 1]) : 0.0) + (i + 1 < n ? std::abs(b[i]) : 0.0));
+    const double pert = std::numeric_limits<double>::epsilon() * std::max(tn, std::numeric_limits<double>::min());
+    // factor P (T - lam I) = L U: U has three diagonals u0, u1, u2; L unit lower with multipliers m
+    std::vector<double> u0(n), u1(n, 0.0), u2(n, 0.0), m(n, 0.0);
+    std::vector<char> swp(n, 0);
+    double dcur = a[0] - lam, ucur = n > 1 ? b[0] : 0.0;  // row i of the remaining matrix: (dcur, ucur) at columns i, i+1
+    for (int i = 0; i + 1 < n; ++i) {
+        const double l = b[i], dn = a[i + 1] - lam, un = i + 2 < n ? b[i + 1] : 0.0;  // row i+1: (l, dn, un)
+        if (std::abs(dcur) >= std::abs(l)) {
+            if (dcur == 0.0) dcur = pert;
+            u0[i] = dcur;
+            u1[i] = ucur;
+            m[i] = l / dcur;
+            dcur = dn - m[i] * ucur;
+            ucur = un;
+        } else {  // rows i and i+1 interchanged
+            swp[i] = 1;
+            u0[i] = l;
+            u1[i] = dn;
+            u2[i] = un;
+            m[i] = dcur / l;
+            const double d2 = ucur - m[i] * dn;
+            ucur = -m[i] * un;
+            dcur = d2;
+        }
+    }
+    u0[n - 1] = dcur == 0.0 ? pert : dcur;
+    auto solve = [&](std::vector<double>& x) {
+        for (int i = 0; i + 1 < n; ++i) {
+            if (swp[i]) std::swap(x[i], x[i + 1]);
+            x[i + 1] -= m[i] * x[i];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double t = x[i];
+            if (i + 1 < n) t -= u1[i] * x[i + 1];
+            if (i + 2 < n) t -= u2[i] * x[i + 2];
+            x[i] = t / u0[i];
+        }
+    };
+    std::vector<double> x(n, 1.0), prev;
+    for (int it = 0; it < 6; ++it) {
+        solve(x);
+        double nr = 0.0;
+        for (double v : x) nr += v * v;
+        nr = std::sqrt(nr);
+        if (!(nr > 0.0) || !std::isfinite(nr)) return tridiag_ground_ql(a, b, n, vec);
+        for (double& v : x) v /= nr;
+        if (it > 0) {
+            double ov = 0.0;
+            for (int i = 0; i < n; ++i) ov += x[i] * prev[i];
+            if (std::abs(std::abs(ov) - 1.0) < 4.0 * std::numeric_limits<double>::epsilon()) break;
+        }
+        prev = x;
+    }
+    // a fixed sign: the largest component positive
+    int im = 0;
+    for (int i = 1; i < n; ++i) if (std::abs(x[i]) > std::abs(x[im])) im = i;
+    if (x[im] < 0) for (double& v : x) v = -v;
+    vec = std::move(x);
+    return lam;
+}
+
+// The same by the QL algorithm with every eigenvector row (O(n^3)): the
+// fallback of tridiag_ground when inverse iteration breaks down.
+double tridiag_ground_ql(const double* a, const double* b, int n, std::vector<double>& vec) {
     if (n <= 0) { vec.clear(); return 0.0; }
     if (n == 1) { vec.assign(1, 1.0); return a[0]; }
     std::vector<int> rows(n);

@@ -20,8 +20,10 @@ double tridiag_lowest(const double* a, const double* b, int n);
 // of eigenvector j.
 void tridiag_eig(const double* a, const double* b, int n, std::vector<double>& evals, const std::vector<int>& rows,
                  std::vector<double>& z);
-// Eigenvector of the lowest eigenvalue (full vector, length n).
+// Lowest eigenvalue and its eigenvector (full vector, length n): Sturm
+// bisection and inverse iteration, O(n); _ql: the same by QL, O(n^3).
 double tridiag_ground(const double* a, const double* b, int n, std::vector<double>& vec);
+double tridiag_ground_ql(const double* a, const double* b, int n, std::vector<double>& vec);
 // Hermitian m x m eigenproblem (cyclic complex Jacobi), ascending eigenvalues;
 // vecs[k][i] = component i of eigenvector k.
 void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, std::vector<std::vector<cd>>& vecs);
