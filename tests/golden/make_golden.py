@@ -74,7 +74,7 @@ def gen_case(ref, name, model, N, sector, terms):
     d["ftlm_alphas"], d["ftlm_betas"], d["ftlm_na"], d["ftlm_nb"], d["ftlm_norms"] = ta, tb, na, nb, nr
     d["ftlm_betas_T"] = BETAS
     d["ftlm_obs"] = np.array([h.ftlm(bt, FTLM_R, FTLM_M) for bt in BETAS])
-    if name == "heis_L16_obc_sz0":  # configs[0]: the published-path Lanczos case; keep it light
+    if name == "heis_L16_obc_sz0":  # the L=16 open-chain Lanczos case: keep its fixture light
         for k in ("csr_ro", "csr_cols", "csr_vals", "x", "y", "cf_phi0", "lanczos_vec"):
             d.pop(k, None)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)

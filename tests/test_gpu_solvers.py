@@ -36,8 +36,8 @@ def test_lanczos_energy(qk, name):
     assert res < 1e-5
 
 
-def test_configs0_heisenberg_L16_obc(qk):
-    """configs[0]: L=16 open chain, Sz=0, tol 1e-12, <=300 iterations; the
+def test_heisenberg_L16_obc_lanczos(qk):
+    """Heisenberg L=16 open chain, Sz=0, tol 1e-12, <=300 iterations; the
     reference gives E0 = -6.911737145574688 (golden heis_L16_obc_sz0)."""
     g = load_golden("heis_L16_obc_sz0")
     H = gpu_ham(qk, g)

@@ -244,7 +244,7 @@ def test_reference_c_api_float_entry_points(qk):
 
 
 def test_full_size_heisenberg_L28_properties(qk, oracle):
-    """configs[1] operator at full size (dim 40,116,600): sampled rows against
+    """Heisenberg L=28 periodic chain, Sz=0, at full size (dim 40,116,600): sampled rows against
     the oracle's CSR rows, Hermiticity, and H 1 = (L/4) 1 (the Sz=0 member of
     the ferromagnetic multiplet)."""
     L = 28
@@ -286,7 +286,7 @@ def test_full_size_heisenberg_L28_properties(qk, oracle):
 
 
 def test_full_size_hubbard_L16_properties(qk):
-    """configs[2] operator at full size (dim 165,636,900): Hermiticity and
+    """Hubbard L=16 periodic chain, half filling, at full size (dim 165,636,900): Hermiticity and
     particle-hole/total-number checks."""
     Lh = 16
     basis, site, ops = make_model(qk, M.HUBBARD, Lh, M.sector(nup=8, ndn=8), M.hubbard_terms(Lh, True))
