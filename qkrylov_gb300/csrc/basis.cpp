@@ -108,7 +108,7 @@ Basis::Basis(Model m, int N_, const Sector& s) : model(m), N(N_), sec(s) {
         if (n_out > kMaxTableBits) {
             // Only tiny sectors of very wide chains are usable; rank them by search.
             rank_kind = RANK_SEARCH;
-            QKG_REQUIRE(k >= 0 && binom(N, k) <= (1ULL << 28), "basis: sector too large for this build");
+            QKG_REQUIRE(k >= 0 && binom(N, k) <= (1ULL << 28), "basis: sector too large for ranking by search (more than 2^28 states)");
             states_int = fixed_pop(N, k);
             dim = states_int.size();
             n_in = N; n_out = 0;
@@ -121,7 +121,7 @@ Basis::Basis(Model m, int N_, const Sector& s) : model(m), N(N_), sec(s) {
         if (sec.use_nup) { gmask[ngroups] = (1ULL << N) - 1; gpop[ngroups] = sec.nup; ++ngroups; }
         if (sec.use_ndn) { gmask[ngroups] = ((1ULL << N) - 1) << N; gpop[ngroups] = sec.ndn; ++ngroups; }
         n_in = N; n_out = N;
-        QKG_REQUIRE(N <= kMaxTableBits, "basis: Hubbard/t-J tables need N <= 22 in this build");
+        QKG_REQUIRE(N <= kMaxTableBits, "basis: Hubbard/t-J rank tables need N <= 22");
         if (m == TJ) {
             rank_kind = RANK_SEARCH;
         } else {
