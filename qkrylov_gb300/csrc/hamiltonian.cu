@@ -15,9 +15,11 @@
 // Work decomposition: rows are grouped into work items that lie inside one
 // outer block (constant high bits a).  Terms are classified at construction:
 //   outer  - flips and conditions only on outer bits: validity and the target
-//            block are the same for every row of the item, so one warp
-//            evaluates them once per item and each row only adds x[row+delta]
-//            (a coalesced, contiguous stream from the neighbouring block);
+//            block are the same for every row of the item, so they are
+//            evaluated once per block (by one warp in the generic kernel, at
+//            construction for the fast kernels) and each row only adds
+//            x[row+delta] (a coalesced, contiguous stream from the
+//            neighbouring block);
 //   inner  - flips and conditions only on inner bits: the target lies in the
 //            same block, rank = block offset + inner_rank[b'];
 //   mixed  - everything else: full rank of the target.
@@ -258,8 +260,10 @@ __global__ void __launch_bounds__(kBlock) spmv_kernel(const SpmvParams<S, A> p, 
 // work item read consecutive table rows) the list of (target inner rank,
 // amplitude index) of the inner terms valid on b, in term order, with their
 // Jordan-Wigner sign folded in.  The table depends only on b, so one copy
-// serves every block.  Outer terms become a per-block list in shared memory;
-// the remaining (straddling) terms are evaluated generically.
+// serves every block.  Outer terms come from a per-block list built at
+// construction (optr/oent); of the remaining (straddling) terms, those whose
+// outer-bit condition holds on the block are listed per block with their
+// target block offset (mptr/ment) and evaluated per row.
 // STAGE: the work item is a whole outer block and its x slice is staged in
 // shared memory, so inner-table gathers read shared memory.
 template <class T, class A, bool REAL, bool UNIF, bool OJ, bool STAGE>
