@@ -3,7 +3,7 @@
  * Part 1 declares every symbol of the reference C API with the reference's
  * names, argument meaning, float signatures and status codes
  * (qkrylov: include/qkrylov/c_api.h:14-168, implemented in src/c_api.cpp);
- * existing callers (the Julia binding's ccall table, bindings/julia/src/*.jl,
+ * existing callers (the Julia binding's ccall table in bindings/julia/src,
  * or any FFI) relink against this library unchanged.  The float entry points
  * run the FP64 GPU engine and cast results to float (the reference compiles
  * its C API into its FP32 engine, CMakeLists.txt:47).
