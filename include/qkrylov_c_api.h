@@ -227,6 +227,12 @@ int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t s
 /* Number of kernels this library has launched so far in the process. */
 uint64_t qkrylov_kernel_launches(void);
 
+/* Bounded device-side waits (a staged SpMV waiting for its asynchronous copy)
+ * that gave up on the current GPU since the process started; waits for that
+ * GPU first.  Returns QKRYLOV_ERROR_DEVICE_TIMEOUT if the count is non-zero
+ * (the results of the affected launches are void), else QKRYLOV_SUCCESS. */
+int qkrylov_device_wait_timeouts(uint32_t* count);
+
 /* Select the GPU for Hamiltonians created afterwards on this thread (the
  * reference's Device(id), include/qkrylov/core/device.hpp:27-45), and wait for
  * all work on the current GPU. */

@@ -113,6 +113,7 @@ _SIGS = {
     "qkrylov_lanczos_ground_state_mixed": (_i, [_vp, _i, _d, _dp, _c.POINTER(LanczosResultF64), _dp]),
     "qkrylov_lanczos_fixed_steps": (_i, [_vp, _i, _u64, _i, _dp, _c.POINTER(LanczosResultF64), _dp]),
     "qkrylov_kernel_launches": (_u64, []),
+    "qkrylov_device_wait_timeouts": (_i, [_c.POINTER(_c.c_uint32)]),
     "qkrylov_vector_dot_device_f64": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_vector_dot_device_f32": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_vector_dot_device_f64_noalloc": (_i, [_vp, _vp, _u64, _dp, _vp]),
@@ -497,6 +498,16 @@ def lanczos_fixed_steps(H, n_steps, seed=0, mixed=True, v0=None, eigenvector_out
 
 def kernel_launches():
     return int(lib().qkrylov_kernel_launches())
+
+
+def device_wait_timeouts():
+    """Bounded device-side waits that gave up on the current GPU (0 when every
+    staged SpMV received its asynchronous copy)."""
+    c = _c.c_uint32()
+    rc = lib().qkrylov_device_wait_timeouts(_c.byref(c))
+    if rc not in (0, -4):
+        _check(rc)
+    return int(c.value)
 
 
 def set_device(device_id):

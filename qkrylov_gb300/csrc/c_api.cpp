@@ -544,6 +544,15 @@ int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t s
 }
 
 uint64_t qkrylov_kernel_launches(void) { return qkg::launch_count(); }
+
+int qkrylov_device_wait_timeouts(uint32_t* count) {
+    if (!count) return QKRYLOV_ERROR_INVALID_ARG;
+    int rc = QKRYLOV_SUCCESS;
+    const int g = guarded([&] { *count = qkg::spmv_wait_timeouts(); });
+    if (g != QKRYLOV_SUCCESS) return g;
+    if (*count) rc = QKRYLOV_ERROR_DEVICE_TIMEOUT;
+    return rc;
+}
 int qkrylov_set_device(int id) {
     return guarded([&] { QKG_CUDA(cudaSetDevice(id)); });
 }

@@ -35,6 +35,10 @@ enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
 enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3, FV_ROWS4_WIDE = 4 };
 constexpr int kFastVariants = 5;
 
+// Bounded device waits of the SpMV kernels that gave up on the current GPU
+// (waits for the GPU first).
+uint32_t spmv_wait_timeouts();
+
 // Device-resident Lanczos step.  The operands of one Lanczos-mode SpMV are kept
 // in device memory and rewritten by the step's last kernel for the next step:
 // y = scale H x - bprev vprev (vprev null: no previous-vector term); the SpMV
@@ -113,8 +117,11 @@ public:
     void set_kernel_mode(int m) { mode_ = m; force_generic_ = (m == 1); }
     void force_generic(bool on) { set_kernel_mode(on ? 1 : 0); }
     // fast-kernel variant for vectors of elem_bytes per element
+    // dynamic shared memory of a staged variant: the largest outer block's slice
+    // of x plus one element on either side (the copy starts on a 16-byte boundary)
+    size_t stage_bytes(size_t elem_bytes) const { return ((max_block_ + 2) * elem_bytes + 15) / 16 * 16; }
     FastVariant variant(size_t elem_bytes) const {
-        const bool can_stage = max_block_ > 0 && max_block_ * elem_bytes <= kStageLimit;
+        const bool can_stage = max_block_ > 0 && stage_bytes(elem_bytes) <= kStageLimit;
         if (mode_ == 2) return FV_ROW;
         if (mode_ == 3) return can_stage ? FV_STAGED : FV_ROW;
         if (mode_ == 4) return FV_ROWS4;

@@ -413,6 +413,44 @@ static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread
 #ifndef QKG_ELL_PREFETCH
 #define QKG_ELL_PREFETCH 1
 #endif
+#ifndef QKG_STAGE_BULK
+#define QKG_STAGE_BULK 1
+#endif
+// Waits on an mbarrier that gave up (bounded spin): counted here, read by the
+// host through spmv_wait_timeouts(); the kernel then computes on whatever the
+// copy delivered, so a non-zero count means the results of that launch are void.
+__device__ unsigned int g_spmv_wait_timeouts;
+constexpr uint32_t kMbarSpinLimit = 1u << 24;  // about a second of polling
+
+// One-shot bulk copy of `bytes` (a multiple of 16, both addresses 16-byte
+// aligned) from global to shared memory, completing on the mbarrier `bar`.
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar), d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
+                 "l"(src), "r"(bytes), "r"(b)
+                 : "memory");
+}
+// Bounded wait for phase 0 of `bar`; false if the limit was reached.
+__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar);
+    for (uint32_t i = 0; i < kMbarSpinLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(b)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 #ifndef QKG_ROWS_MINB_WIDE
 #define QKG_ROWS_MINB_WIDE 4
 #endif
@@ -439,8 +477,29 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     __shared__ A s_iamp[2 * kMaxInnerTable];
     const WorkItem it = p.items[blockIdx.x];
     const uint32_t block_off = __ldg(p.outer_off + it.a);
-    if (STAGE)  // the item is the whole outer block: rows [block_off, block_off + count)
-        for (uint32_t i = threadIdx.x; i < it.count; i += blockDim.x) xs[i] = x[block_off + i];
+    // STAGE: the item is the whole outer block, rows [block_off, block_off +
+    // count); xs holds x from the even index st0 = block_off & ~1 on, so row i
+    // of the block is xst[i] = xs[(block_off & 1) + i]
+    const T2* xst = xs + (block_off & 1u);
+#if QKG_STAGE_BULK
+    // the slice arrives by one asynchronous bulk copy (TMA engine) issued
+    // before the outer terms are summed and waited for before the inner walk
+    __shared__ unsigned long long s_bar;
+    bool bulk = false;
+    if (STAGE) {
+        const uint32_t st0 = block_off & ~1u, end = (block_off + it.count) & ~1u;  // [st0, end): whole 16-byte pairs
+        bulk = end > st0 && (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
+        if (bulk) {
+            if (threadIdx.x == 0) mbar_init(&s_bar);
+            if (threadIdx.x == 32 && end < block_off + it.count) xs[end - st0] = x[end];  // odd last row
+        } else {
+            for (uint32_t i = threadIdx.x; i < it.count; i += blockDim.x) xs[(block_off & 1u) + i] = x[block_off + i];
+        }
+    }
+#else
+    if (STAGE)
+        for (uint32_t i = threadIdx.x; i < it.count; i += blockDim.x) xs[(block_off & 1u) + i] = x[block_off + i];
+#endif
     if (!UNIF) {
         const uint32_t sa = it.a << p.n_in;
         for (int t = threadIdx.x; t < p.n_inner; t += blockDim.x) {
@@ -451,6 +510,12 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         }
     }
     if (STAGE || !UNIF) __syncthreads();
+#if QKG_STAGE_BULK
+    if (STAGE && bulk && threadIdx.x == 0) {
+        const uint32_t st0 = block_off & ~1u, end = (block_off + it.count) & ~1u;
+        bulk_g2s(xs, x + st0, (end - st0) * (uint32_t)sizeof(T2), &s_bar);
+    }
+#endif
     // this block's outer entries and straddling terms (with their target block
     // offsets), listed per outer configuration at construction
     const uint32_t o0 = __ldg(p.optr + it.a), o1 = __ldg(p.optr + it.a + 1);
@@ -498,6 +563,12 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         }
     }
     // the four rows' ELL walks, slot by slot
+#if QKG_STAGE_BULK
+    if (STAGE && bulk && pass == 0 && !mbar_wait0(&s_bar)) {
+        atomicAdd(&g_spmv_wait_timeouts, 1u);
+        mbar_wait0(&s_bar);  // the copy may still be writing shared memory: wait once more
+    }
+#endif
 #if QKG_ELL_PREFETCH
     // the next slot's entries are loaded while this slot's gathers are in flight
     uint32_t cur[RT];
@@ -511,7 +582,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         for (int q = 0; q < RT; ++q) {
             e0[q] += 32;
             nxt[q] = (cur[q] != kEllEmpty && e0[q] < e1[q]) ? __ldg(p.ient + e0[q]) : kEllEmpty;
-            if (cur[q] != kEllEmpty) xv[q] = STAGE ? xs[cur[q] & rmask] : x[block_off + (cur[q] & rmask)];
+            if (cur[q] != kEllEmpty) xv[q] = STAGE ? xst[cur[q] & rmask] : x[block_off + (cur[q] & rmask)];
         }
         more = false;
 #pragma unroll
@@ -546,7 +617,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         T2 xv[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q)
-            if (ent[q] != kEllEmpty) xv[q] = STAGE ? xs[ent[q] & rmask] : x[block_off + (ent[q] & rmask)];
+            if (ent[q] != kEllEmpty) xv[q] = STAGE ? xst[ent[q] & rmask] : x[block_off + (ent[q] & rmask)];
 #pragma unroll
         for (int q = 0; q < RT; ++q) {
             if (ent[q] == kEllEmpty) {
@@ -608,7 +679,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         const uint32_t row = (uint32_t)it.row0 + rl;
         dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
                                        : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
-        xd[q] = STAGE ? xs[rl] : x[row];
+        xd[q] = STAGE ? xst[rl] : x[row];
         if (vprev) pv[q] = vprev[row];
     }
 #pragma unroll
@@ -1023,8 +1094,8 @@ void Hamiltonian::build_fast() {
     for (const auto& w : bitems) max_block_ = std::max<size_t>(max_block_, w.count);
     n_items_blk_ = bitems.size();
     upload_vec(items_blk_, bitems);
-    if (max_block_ * 8 <= kStageLimit) allow_stage_smem<float, float>(std::max<size_t>(max_block_ * 8, 1));
-    if (max_block_ * 16 <= kStageLimit) allow_stage_smem<double, double>(std::max<size_t>(max_block_ * 16, 1));
+    if (stage_bytes(8) <= kStageLimit) allow_stage_smem<float, float>(stage_bytes(8));
+    if (stage_bytes(16) <= kStageLimit) allow_stage_smem<double, double>(stage_bytes(16));
     fast_ = true;
     autotune();
 }
@@ -1044,7 +1115,7 @@ void Hamiltonian::autotune() {
         QKG_CUDA(cudaEventCreate(&b));
         double best = 0.0;
         for (int v = 0; v < kFastVariants; ++v) {
-            if ((v == FV_STAGED || v == FV_ROWS4_STAGED) && !(max_block_ * e <= kStageLimit)) continue;
+            if ((v == FV_STAGED || v == FV_ROWS4_STAGED) && !(stage_bytes(e) <= kStageLimit)) continue;
             mode_ = 2 + v;  // modes 2..6 select variants 0..4
             auto run = [&] {
                 if (prec) apply_f64(x.as<double2>(), y.as<double2>(), stream_);
@@ -1193,6 +1264,13 @@ void Hamiltonian::fast_params(FastParams<A>& p) const {
     p.dtab = dtab.as<A>();
 }
 template void Hamiltonian::fast_params<float>(FastParams<float>&) const;
+uint32_t spmv_wait_timeouts() {
+    QKG_CUDA(cudaDeviceSynchronize());
+    uint32_t c = 0;
+    QKG_CUDA(cudaMemcpyFromSymbol(&c, g_spmv_wait_timeouts, sizeof(c)));
+    return c;
+}
+
 DBuf& Hamiltonian::krylov_workspace(size_t bytes) const {
     if (kws_.bytes < bytes) {
         kws_.reset();  // free first: the old and new spaces need not fit together
@@ -1420,7 +1498,7 @@ void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const 
         fast_params(p);
         size_t ni = 0;
         p.items = items_of(v, &ni);
-        launch_fast<double, double>(p, ni, all_real_, unif_, x, y, s, v, st ? max_block_ * 16 : 0);
+        launch_fast<double, double>(p, ni, all_real_, unif_, x, y, s, v, st ? stage_bytes(16) : 0);
         return;
     }
     const DBuf& full = dfull64_;
@@ -1440,7 +1518,7 @@ void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) cons
     p.items = items_of(v, &ni);
     p.lz = lz.op;
     p.apart = lz.apart;
-    launch_fast<float, float>(p, ni, all_real_, unif_, nullptr, nullptr, s, v, st ? max_block_ * 8 : 0);
+    launch_fast<float, float>(p, ni, all_real_, unif_, nullptr, nullptr, s, v, st ? stage_bytes(8) : 0);
 }
 
 size_t Hamiltonian::lanczos_parts() const {
@@ -1467,7 +1545,7 @@ void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
         fast_params(p);
         size_t ni = 0;
         p.items = items_of(v, &ni);
-        launch_fast<float, float>(p, ni, all_real_, unif_, x, y, s, v, st ? max_block_ * 8 : 0);
+        launch_fast<float, float>(p, ni, all_real_, unif_, x, y, s, v, st ? stage_bytes(8) : 0);
         return;
     }
     if (wide_)

@@ -132,6 +132,8 @@ def test_apply_against_oracle(qk, oracle, model, N, sector, terms):
         assert np.abs(y - yo).max() <= RTOL64 * np.abs(yo).max()
         y32 = apply32(qk, H, x)
         assert np.abs(y32 - yo).max() <= RTOL32 * 10 * np.abs(yo).max()
+    # the staged kernels' bounded waits for their asynchronous copies never gave up
+    assert qk.device_wait_timeouts() == 0
 
 
 def test_edge_cases(qk):
