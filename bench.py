@@ -402,6 +402,8 @@ def cf_batch(qk, hbm_peak, peak_kind):
         P[i] = ph
     phis = P
     omegas = np.linspace(0.0, 4.0, CF_NOMEGA)
+    for mixed in (True, False):  # warm-up: tile autotuning and the block workspace
+        qk.spectral_functions_block(H, phis, omegas[:2], E0, eta=CF_ETA, n_iter=3, mixed=mixed)
     out = {}
     for mixed in (True, False):
         t0 = time.perf_counter()
