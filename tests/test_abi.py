@@ -71,6 +71,13 @@ def test_sector_semantics(qk):
     r = qk.LanczosResultC()
     assert L.qkrylov_lanczos_ground_state(None, 10, 1e-8, ctypes.byref(r)) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_evaluate_spectral_function(None, None, 0, 1.0, 0.0, 0.0, 0.1) == 0.0
+    # additions: invalid arguments are rejected before any device work
+    held = ctypes.c_uint64()
+    assert L.qkrylov_hamiltonian_workspace(None, 0, ctypes.byref(held)) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_hamiltonian_workspace(None, 1, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_device_wait_timeouts(None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_hamiltonian_benchmark_apply(None, 1, 3, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_hamiltonian_tuning(None, 1, None, None) == qk.ERROR_INVALID_ARG
 
 
 @pytest.mark.parametrize("name", golden_names())
