@@ -660,7 +660,11 @@ double qkrylov_evaluate_spectral_function_f64(const double* alphas, const double
 int qkrylov_evaluate_spectral_grid_f64(const double* alphas, const double* betas, size_t n, double norm,
                                        const double* omegas, size_t n_omega, double E0, double eta, double* out) {
     if (!alphas || !betas || !omegas || !out) return QKRYLOV_ERROR_INVALID_ARG;
-    for (size_t k = 0; k < n_omega; ++k) out[k] = n ? qkg::spectral(alphas, betas, n, norm, omegas[k], E0, eta) : 0.0;
+    // frequencies are independent: spread large grids over the host cores
+    // (each value is computed exactly as in the serial loop)
+#pragma omp parallel for schedule(static) if (n_omega * (n + 1) >= 65536)
+    for (long long k = 0; k < (long long)n_omega; ++k)
+        out[k] = n ? qkg::spectral(alphas, betas, n, norm, omegas[k], E0, eta) : 0.0;
     return QKRYLOV_SUCCESS;
 }
 
