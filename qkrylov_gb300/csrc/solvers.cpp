@@ -939,6 +939,7 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
                 // FP64 refinement: Rayleigh quotient and residual of each normalised Ritz vector
                 V.clear();
                 HV.clear();
+                pool.free.clear();  // give the basis memory back before the FP64 vectors
                 e64.alloc(n * sizeof(double2));
                 h64.alloc(n * sizeof(double2));
                 bool conv64 = true;
