@@ -141,3 +141,19 @@ def test_opsum_python_sugar(qk):
     assert os_.terms[1] == (0.5 + 0j, [("Sp", 0), ("Sm", 1)])
     with pytest.raises(ValueError):
         os_ += (1.0, "Sz")
+
+
+def test_spectral_grid_equals_pointwise(qk):
+    """The frequency grid (evaluated in parallel for large grids) gives, value for
+    value, the single-frequency continued fraction (dynamics.cpp:61-89)."""
+    rng = np.random.default_rng(5)
+
+    class R:
+        pass
+    r = R()
+    r.alphas, r.betas, r.norm_phi0 = rng.normal(size=120), np.abs(rng.normal(size=120)), 0.8
+    om = np.linspace(-1.0, 5.0, 1200)
+    grid = qk.evaluate_spectral_function(r, om, -3.0, 0.07)
+    point = np.array([qk.evaluate_spectral_function(r, float(w), -3.0, 0.07) for w in om[::37]])
+    np.testing.assert_array_equal(grid[::37], point)
+    assert np.all(grid >= 0)
