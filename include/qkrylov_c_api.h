@@ -187,7 +187,11 @@ int qkrylov_vector_dot_device_f32(const void* d_x, const void* d_y, uint64_t n, 
  * elements; larger n returns QKRYLOV_ERROR_INVALID_ARG.  All calls share that
  * array: calls that overlap on the GPU race and must be serialised by the
  * caller.  The first call on a GPU looks up the array's address there and
- * should come before any stream capture. */
+ * loads the call's kernels; under CUDA's lazy module loading that is when the
+ * array and the kernels take their device memory, so make one call with n = 0
+ * (the warm-up: it computes nothing) before reserving the GPU's memory.  The
+ * call waits for `stream` to read the result, so it cannot be used inside a
+ * stream capture. */
 int qkrylov_vector_dot_device_f64_noalloc(const void* d_x, const void* d_y, uint64_t n, double* result,
                                           void* stream);
 
@@ -216,8 +220,10 @@ int qkrylov_lanczos_ground_state_f64(qkrylov_hamiltonian_h h, int maxiter, doubl
  * refined value. */
 int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, double tol, const double* v0_complex,
                                        qkrylov_lanczos_result_f64_t* result, double* eigenvector_complex);
-/* Performance form of both: exactly n_steps steps (no early exit); mixed != 0
- * selects the mixed form.  The start vector is v0_complex (host, reference
+/* Performance form of both: exactly n_steps steps (no early exit); mixed = 1
+ * selects the mixed form, 0 the FP64 form with full reorthogonalisation and 2
+ * the FP64 form with the mixed form's selective reorthogonalisation (against
+ * the lowest Ritz vector once it has converged to sqrt(eps_64) ||T||).  The start vector is v0_complex (host, reference
  * order) if given, else a seeded device Gaussian (Philox4x32-10, `seed`).
  * eigenvector_complex (host, optional) receives the Ritz vector. */
 int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed,
@@ -229,9 +235,25 @@ uint64_t qkrylov_kernel_launches(void);
 
 /* Bounded device-side waits (a staged SpMV waiting for its asynchronous copy)
  * that gave up on the current GPU since the process started; waits for that
- * GPU first.  Returns QKRYLOV_ERROR_DEVICE_TIMEOUT if the count is non-zero
- * (the results of the affected launches are void), else QKRYLOV_SUCCESS. */
+ * GPU first.  Returns QKRYLOV_ERROR_DEVICE_TIMEOUT if the count is non-zero,
+ * else QKRYLOV_SUCCESS.  A kernel whose wait gave up reads its operand from
+ * global memory instead, so its results are complete; a solver call during
+ * which the count grew returns QKRYLOV_ERROR_DEVICE_TIMEOUT. */
 int qkrylov_device_wait_timeouts(uint32_t* count);
+
+/* Test hooks (no counterpart in the reference).
+ * qkrylov_debug_inject_alloc_failure: the after_n-th device allocation of the
+ * library from now on (0: the next one) fails as cudaMalloc does on an
+ * exhausted GPU; -1 switches the injection off.  Creators then return NULL and
+ * other calls QKRYLOV_ERROR_CUDA, with qkrylov_last_error() set.
+ * qkrylov_debug_live_allocations: device allocations the library holds now.
+ * qkrylov_debug_device_wait_probe: one kernel waits on an mbarrier that nothing
+ * completes, for limit_ns of GPU global time (clamped to 1 us .. 1 s), and
+ * counts the give-up as qkrylov_device_wait_timeouts does; no copy is in
+ * flight, the GPU stays usable. */
+int qkrylov_debug_inject_alloc_failure(int64_t after_n);
+int64_t qkrylov_debug_live_allocations(void);
+int qkrylov_debug_device_wait_probe(int64_t limit_ns);
 
 /* Select the GPU for Hamiltonians created afterwards on this thread (the
  * reference's Device(id), include/qkrylov/core/device.hpp:27-45), and wait for
@@ -290,7 +312,10 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* n_outer, int* n_inner
  * kernel with shared-memory staging of each outer block's slice of x (when a
  * block fits); 4 the fast kernel with four rows per thread; 5 four rows per
  * thread with the block staged (when it fits); 6 four rows per thread with a
- * larger register budget.
+ * larger register budget; 7, 8, 9 the tiled kernel over 1, 2, 4 outer blocks
+ * per CTA (the blocks' slices of x in shared memory; when they fit); 10 the
+ * class-persistent kernel (one CTA per SM, inner table and slices of x in
+ * shared memory; when they fit).
  * *fast_in_use (optional) reports whether the fast kernel applies. */
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use);
 
@@ -299,8 +324,14 @@ int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int*
  * rows per thread staged, 4 four rows per thread wide; -1 when the generic kernel
  * applies) and the autotuner's mean launch times per variant
  * (ms_per_variant[5], 0 = not measured; sectors below 2^20 rows are not
- * timed). */
+ * timed).  *variant is 5 when mode 0 uses a variant added later (see
+ * qkrylov_hamiltonian_tuning_ex). */
 int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, double* ms_per_variant);
+
+/* The same with every variant: *variant 0..4 as above, 5, 6, 7 the tiled
+ * kernel over 1, 2, 4 outer blocks per CTA, 8 the class-persistent kernel; ms_per_variant receives n_ms
+ * entries (variants beyond those the library has read 0). */
+int qkrylov_hamiltonian_tuning_ex(qkrylov_hamiltonian_h h, int fp32, int* variant, double* ms_per_variant, int n_ms);
 
 /* States first .. first + count - 1 of a basis in the reference's order and
  * bit encoding (qkrylov_basis_state for a range). */

@@ -43,49 +43,89 @@ inline double jw(uint64_t state, int bit) {  // fermion_site.cpp:143-154, hubbar
     return (popc(state & mask) % 2 == 0) ? 1.0 : -1.0;
 }
 
-// Site actions, one per model.
-LocalAction site_apply(int model, const std::string& op, int site, uint64_t state) {
+// Site actions, one per model.  The operator name is looked up once per
+// factor (op_id); an unknown name gets id -1 and throws when first applied,
+// which is when the reference's site.apply throws (its CSR build applies the
+// factors of a term in order and stops at the first invalid one).
+enum : int { OP_SZ, OP_SP, OP_SM, OP_SX, OP_SY, OP_N, OP_ID, OP_C, OP_CDAG, OP_NUP, OP_NDN, OP_NUPDN, OP_CUP,
+             OP_CDAGUP, OP_CDN, OP_CDAGDN };
+int op_id(int model, const std::string& op) {
+    if (model == 0) {  // src/sites/spinhalf_site.cpp:18-121
+        if (op == "Sz") return OP_SZ;
+        if (op == "Sp") return OP_SP;
+        if (op == "Sm") return OP_SM;
+        if (op == "Sx") return OP_SX;
+        if (op == "Sy") return OP_SY;
+        return -1;
+    }
+    if (model == 1) {  // src/sites/fermion_site.cpp:19-84
+        if (op == "N") return OP_N;
+        if (op == "Id") return OP_ID;
+        if (op == "C") return OP_C;
+        if (op == "Cdag") return OP_CDAG;
+        return -1;
+    }
+    if (op == "Nup") return OP_NUP;
+    if (op == "Ndn") return OP_NDN;
+    if (model != 3 && op == "Nupdn") return OP_NUPDN;
+    if (op == "CUp") return OP_CUP;
+    if (op == "CdagUp") return OP_CDAGUP;
+    if (op == "CDn") return OP_CDN;
+    if (op == "CdagDn") return OP_CDAGDN;
+    return -1;
+}
+[[noreturn]] void unknown_op(int model, const std::string& op) {
+    if (model == 0) throw std::runtime_error("Unknown spin operator: " + op);
+    if (model == 1) throw std::runtime_error("Unknown fermion operator: " + op);
+    throw std::runtime_error(std::string(model == 3 ? "Unknown TJ operator: " : "Unknown Hubbard operator: ") + op);
+}
+LocalAction site_apply_id(int model, int id, const std::string& op, int site, uint64_t state) {
     LocalAction a;
+    if (id < 0) unknown_op(model, op);
     if (model == 0) {  // src/sites/spinhalf_site.cpp:18-121
         const bool up = (state >> site) & 1ULL;
-        if (op == "Sz") { a.valid = true; a.new_state = state; a.element = up ? 0.5 : -0.5; return a; }
-        if (op == "Sp") { if (up) return a; a.valid = true; a.new_state = state | (1ULL << site); a.element = 1.0; return a; }
-        if (op == "Sm") { if (!up) return a; a.valid = true; a.new_state = state & ~(1ULL << site); a.element = 1.0; return a; }
-        if (op == "Sx") { a.valid = true; a.new_state = state ^ (1ULL << site); a.element = 0.5; return a; }
-        if (op == "Sy") {
-            a.valid = true; a.new_state = state ^ (1ULL << site);
-            a.element = up ? cd(0.0, -0.5) : cd(0.0, 0.5);
-            return a;
+        switch (id) {
+            case OP_SZ: a.valid = true; a.new_state = state; a.element = up ? 0.5 : -0.5; return a;
+            case OP_SP: if (up) return a; a.valid = true; a.new_state = state | (1ULL << site); a.element = 1.0; return a;
+            case OP_SM: if (!up) return a; a.valid = true; a.new_state = state & ~(1ULL << site); a.element = 1.0; return a;
+            case OP_SX: a.valid = true; a.new_state = state ^ (1ULL << site); a.element = 0.5; return a;
+            default:  // OP_SY
+                a.valid = true; a.new_state = state ^ (1ULL << site);
+                a.element = up ? cd(0.0, -0.5) : cd(0.0, 0.5);
+                return a;
         }
-        throw std::runtime_error("Unknown spin operator: " + op);
     }
     if (model == 1) {  // src/sites/fermion_site.cpp:19-84
         const bool occ = (state >> site) & 1ULL;
-        if (op == "N") { a.valid = true; a.new_state = state; a.element = occ ? 1.0 : 0.0; return a; }
-        if (op == "Id") { a.valid = true; a.new_state = state; a.element = 1.0; return a; }
-        if (op == "C") { if (!occ) return a; a.valid = true; a.new_state = state & ~(1ULL << site); a.element = jw(state, site); return a; }
-        if (op == "Cdag") { if (occ) return a; a.valid = true; a.new_state = state | (1ULL << site); a.element = jw(state, site); return a; }
-        throw std::runtime_error("Unknown fermion operator: " + op);
+        switch (id) {
+            case OP_N: a.valid = true; a.new_state = state; a.element = occ ? 1.0 : 0.0; return a;
+            case OP_ID: a.valid = true; a.new_state = state; a.element = 1.0; return a;
+            case OP_C: if (!occ) return a; a.valid = true; a.new_state = state & ~(1ULL << site); a.element = jw(state, site); return a;
+            default:  // OP_CDAG
+                if (occ) return a; a.valid = true; a.new_state = state | (1ULL << site); a.element = jw(state, site); return a;
+        }
     }
     // Hubbard (src/sites/hubbard_site.cpp:51-125) and t-J (src/sites/tj_site.cpp:176-242):
     // up electron of site i at bit 2i, down electron at bit 2i+1.
     const int bu = 2 * site, bd = 2 * site + 1;
     const bool up = (state >> bu) & 1ULL, dn = (state >> bd) & 1ULL;
     const bool tj = (model == 3);
-    if (op == "Nup") { a.valid = true; a.new_state = state; a.element = up ? 1.0 : 0.0; return a; }
-    if (op == "Ndn") { a.valid = true; a.new_state = state; a.element = dn ? 1.0 : 0.0; return a; }
-    if (!tj && op == "Nupdn") { a.valid = true; a.new_state = state; a.element = (up && dn) ? 1.0 : 0.0; return a; }
-    if (op == "CUp") { if (!up) return a; a.valid = true; a.new_state = state & ~(1ULL << bu); a.element = jw(state, bu); return a; }
-    if (op == "CdagUp") {
-        if (up || (tj && dn)) return a;  // t-J forbids double occupancy (tj_site.cpp:214)
-        a.valid = true; a.new_state = state | (1ULL << bu); a.element = jw(state, bu); return a;
+    switch (id) {
+        case OP_NUP: a.valid = true; a.new_state = state; a.element = up ? 1.0 : 0.0; return a;
+        case OP_NDN: a.valid = true; a.new_state = state; a.element = dn ? 1.0 : 0.0; return a;
+        case OP_NUPDN: a.valid = true; a.new_state = state; a.element = (up && dn) ? 1.0 : 0.0; return a;
+        case OP_CUP: if (!up) return a; a.valid = true; a.new_state = state & ~(1ULL << bu); a.element = jw(state, bu); return a;
+        case OP_CDAGUP:
+            if (up || (tj && dn)) return a;  // t-J forbids double occupancy (tj_site.cpp:214)
+            a.valid = true; a.new_state = state | (1ULL << bu); a.element = jw(state, bu); return a;
+        case OP_CDN: if (!dn) return a; a.valid = true; a.new_state = state & ~(1ULL << bd); a.element = jw(state, bd); return a;
+        default:  // OP_CDAGDN
+            if (dn || (tj && up)) return a;  // tj_site.cpp:232
+            a.valid = true; a.new_state = state | (1ULL << bd); a.element = jw(state, bd); return a;
     }
-    if (op == "CDn") { if (!dn) return a; a.valid = true; a.new_state = state & ~(1ULL << bd); a.element = jw(state, bd); return a; }
-    if (op == "CdagDn") {
-        if (dn || (tj && up)) return a;  // tj_site.cpp:232
-        a.valid = true; a.new_state = state | (1ULL << bd); a.element = jw(state, bd); return a;
-    }
-    throw std::runtime_error(std::string(tj ? "Unknown TJ operator: " : "Unknown Hubbard operator: ") + op);
+}
+LocalAction site_apply(int model, const std::string& op, int site, uint64_t state) {
+    return site_apply_id(model, op_id(model, op), op, site, state);
 }
 
 struct Sector { bool use_sz = false; int sz2 = 0; bool use_nup = false, use_ndn = false; int nup = 0, ndn = 0; bool use_n = false; int n = 0; };
@@ -115,13 +155,38 @@ inline uint64_t interleave(uint64_t up, uint64_t dn, int N) {
 struct Basis {
     int model = 0, N = 0;
     std::vector<uint64_t> states;
+    int fixed_k = -1;  // spin/fermion sector of fixed popcount: states are all N-bit strings with k ones
     uint64_t size() const { return states.size(); }
     int64_t index(uint64_t s) const {
         auto it = std::lower_bound(states.begin(), states.end(), s);
         if (it == states.end() || *it != s) return -1;
         return it - states.begin();
     }
+    // index() by the colex rank where the basis is a fixed-popcount class (the
+    // ascending order of such a class is its colex order), else index().
+    int64_t index_fast(uint64_t s) const;
 };
+
+uint64_t binom64(int n, int k) {
+    static const std::vector<uint64_t> tab = [] {
+        std::vector<uint64_t> t(65 * 65, 0);
+        for (int a = 0; a <= 64; ++a) {
+            t[a * 65] = 1;
+            for (int b = 1; b <= a; ++b) t[a * 65 + b] = t[(a - 1) * 65 + b - 1] + (b <= a - 1 ? t[(a - 1) * 65 + b] : 0);
+        }
+        return t;
+    }();
+    return (k < 0 || k > n) ? 0 : tab[n * 65 + k];
+}
+
+int64_t Basis::index_fast(uint64_t s) const {
+    if (fixed_k < 0) return index(s);
+    if (popc(s) != fixed_k || (N < 64 && (s >> N) != 0)) return -1;
+    uint64_t r = 0;
+    int i = 0;
+    for (uint64_t t = s; t; t &= t - 1) r += binom64(__builtin_ctzll(t), ++i);
+    return (int64_t)r;
+}
 
 // src/basis/spinhalf_basis.cpp:12-30,59-104; fermion_basis.cpp:12-89;
 // hubbard_basis.cpp:12-100; tj_basis.cpp:12-96.
@@ -136,10 +201,12 @@ Basis build_basis(int model, int N, const Sector& sec) {
             for (uint64_t s = 0; s < dim; ++s) b.states[s] = s;
         } else if (model == 0) {
             // 2*popcount - N == sz2  (spinhalf_basis.cpp:72-84)
-            if ((sec.sz2 + N) % 2 == 0) b.states = fixed_pop(N, (sec.sz2 + N) / 2);
+            if ((sec.sz2 + N) % 2 == 0) { b.states = fixed_pop(N, (sec.sz2 + N) / 2); b.fixed_k = (sec.sz2 + N) / 2; }
         } else {
             b.states = fixed_pop(N, sec.n);
+            b.fixed_k = sec.n;
         }
+        if (b.states.empty()) b.fixed_k = -1;
         return b;
     }
     if (N <= 0 || N > 31) throw std::runtime_error("basis: N must satisfy 1 <= N <= 31");
@@ -159,7 +226,7 @@ Basis build_basis(int model, int N, const Sector& sec) {
     return b;
 }
 
-struct Factor { std::string op; int site; };
+struct Factor { std::string op; int site; int id = -1; };
 struct Term { cd coeff; std::vector<Factor> factors; };
 
 struct Ham {
@@ -186,7 +253,7 @@ void build_csr(Ham& h, uint64_t row0, uint64_t nrows) {
         for (const auto& t : h.terms) {
             uint64_t s = s0; cd amp = t.coeff; bool valid = true;
             for (const auto& f : t.factors) {
-                auto a = site_apply(h.basis.model, f.op, f.site, s);
+                auto a = site_apply_id(h.basis.model, f.id, f.op, f.site, s);
                 if (!a.valid) { valid = false; break; }
                 s = a.new_state; amp *= a.element;
             }
@@ -200,6 +267,67 @@ void build_csr(Ham& h, uint64_t row0, uint64_t nrows) {
         }
     }
     h.rows[nrows] = (int32_t)h.cols.size();
+}
+
+// The same CSR as build_csr(h, 0, dim) (same rows, entries in the same order),
+// built by all host threads in two passes (count, then fill) with the colex
+// rank where the basis allows it.  Used where the reference's single-threaded
+// assembly would take minutes (the CPU baseline at full size); the CSR build is
+// not part of the timed work.
+void build_csr_parallel(Ham& h) {
+    const uint64_t n = h.basis.size();
+    h.row0 = 0; h.nrows = n;
+    h.rows.assign(n + 1, 0);
+    h.diag.assign(n, cd(0.0, 0.0));
+    std::vector<int32_t> cnt(n, 0);
+    auto row_entries = [&](uint64_t alpha, auto&& emit) {
+        const uint64_t s0 = h.basis.states[alpha];
+        for (const auto& t : h.terms) {
+            uint64_t s = s0; cd amp = t.coeff; bool valid = true;
+            for (const auto& f : t.factors) {
+                auto a = site_apply_id(h.basis.model, f.id, f.op, f.site, s);
+                if (!a.valid) { valid = false; break; }
+                s = a.new_state; amp *= a.element;
+            }
+            if (!valid) continue;
+            const int64_t beta = h.basis.index_fast(s);
+            if (beta < 0) continue;
+            emit(beta, cd(amp.real(), -amp.imag()));
+        }
+    };
+    std::string err;
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long r = 0; r < (long long)n; ++r) {
+        try {
+            int32_t c = 0;
+            row_entries((uint64_t)r, [&](int64_t, cd) { ++c; });
+            cnt[r] = c;
+        } catch (const std::exception& e) {
+#pragma omp critical
+            err = e.what();
+        }
+    }
+    if (!err.empty()) throw std::runtime_error(err);
+    uint64_t total = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        h.rows[r] = (int32_t)total;
+        total += (uint64_t)cnt[r];
+        if (total > 0x7fffffffULL) throw std::runtime_error("CSR: more than 2^31-1 entries (int32 offsets)");
+    }
+    h.rows[n] = (int32_t)total;
+    std::vector<int32_t>().swap(cnt);
+    h.cols.resize(total);
+    h.vals.resize(total);
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long r = 0; r < (long long)n; ++r) {
+        int64_t k = h.rows[r];
+        row_entries((uint64_t)r, [&](int64_t beta, cd val) {
+            h.cols[k] = (int32_t)beta;
+            h.vals[k] = val;
+            ++k;
+            if (beta == r) h.diag[r] += val;
+        });
+    }
 }
 
 // ---- vector algebra: include/qkrylov/linalg/vector_ops.hpp:14-137 --------------
@@ -335,7 +463,7 @@ void fill_complex(std::mt19937& rng, Dist& dist, uint64_t n, cd* out) {
 // ---- Lanczos: src/solvers/lanczos.cpp:101-202 -------------------------------------
 struct LanczosOut { double energy = 0; int iters = 0; bool conv = false; Vec evec; std::vector<double> alphas, betas; };
 
-LanczosOut lanczos(const Ham& H, Vec v_curr, int maxiter, double tol) {
+LanczosOut lanczos(const Ham& H, Vec v_curr, int maxiter, double tol, std::vector<double>* step_s = nullptr) {
     LanczosOut out;
     const uint64_t dim = H.basis.size();
     if (dim == 0) return out;
@@ -347,8 +475,16 @@ LanczosOut lanczos(const Ham& H, Vec v_curr, int maxiter, double tol) {
     std::vector<double>& betas = out.betas;
     bool conv = false; double e_old = 1e100; int iters = 0;
     const int nmax = std::min<int>(maxiter, (int)dim);
+    auto t_step = std::chrono::steady_clock::now();
+    auto lap = [&] {
+        if (!step_s) return;
+        const auto now = std::chrono::steady_clock::now();
+        step_s->push_back(std::chrono::duration<double>(now - t_step).count());
+        t_step = now;
+    };
     for (int iter = 0; iter < nmax; ++iter) {
         iters = iter + 1;
+        t_step = std::chrono::steady_clock::now();
         apply(H, v_curr, w);
         const double alpha = dot(v_curr, w).real();
         alphas.push_back(alpha);
@@ -356,8 +492,8 @@ LanczosOut lanczos(const Ham& H, Vec v_curr, int maxiter, double tol) {
         if (iter > 0) axpy(cd(-betas.back(), 0.0), v_prev, w);
         for (const auto& bv : V) axpy(-dot(bv, w), bv, w);  // full reorthogonalisation (:148-151)
         const double beta = norm(w);
-        if (beta < 1e-15) { conv = true; break; }
-        if (iter + 1 == nmax) break;
+        if (beta < 1e-15) { conv = true; lap(); break; }
+        if (iter + 1 == nmax) { lap(); break; }
         betas.push_back(beta);
         v_prev = v_curr;
         v_curr = w;
@@ -366,9 +502,10 @@ LanczosOut lanczos(const Ham& H, Vec v_curr, int maxiter, double tol) {
         if (iter > 0) {
             std::vector<double> tv;
             const double e = tridiag_ground(alphas, betas, (int)alphas.size(), tv);
-            if (std::abs(e - e_old) < tol) { e_old = e; conv = true; break; }
+            if (std::abs(e - e_old) < tol) { e_old = e; conv = true; lap(); break; }
             e_old = e;
         }
+        lap();
     }
     std::vector<double> ev;
     out.energy = tridiag_ground(alphas, betas, (int)alphas.size(), ev);
@@ -427,7 +564,9 @@ SmallEig small_hermitian(const std::vector<std::vector<cd>>& Hm) {  // :22-82 (c
 
 struct DavidsonOut { std::vector<double> vals; std::vector<Vec> vecs; int iters = 0; bool conv = false; };
 
-DavidsonOut davidson(const Ham& H, int n_eig, int max_sub, double tol) {  // :86-227
+// max_iter: the reference's hard-coded 100 (:141,180); the CPU baseline times
+// fewer iterations of the same loop.
+DavidsonOut davidson(const Ham& H, int n_eig, int max_sub, double tol, int max_iter = 100) {  // :86-227
     DavidsonOut out;
     const uint64_t dim = H.basis.size();
     if (dim == 0) return out;
@@ -455,7 +594,7 @@ DavidsonOut davidson(const Ham& H, int n_eig, int max_sub, double tol) {  // :86
         apply(H, v, hv);
         HV.push_back(hv);
     }
-    for (int iter = 0; iter < 100; ++iter) {
+    for (int iter = 0; iter < max_iter; ++iter) {
         const int m = (int)V.size();
         std::vector<std::vector<cd>> Hs(m, std::vector<cd>(m));
         for (int i = 0; i < m; ++i)
@@ -486,7 +625,7 @@ DavidsonOut davidson(const Ham& H, int n_eig, int max_sub, double tol) {  // :86
                 corr.push_back(std::move(t));
             }
         }
-        if (all_conv || iter == 99) {
+        if (all_conv || iter == max_iter - 1) {
             out.iters = iter + 1; out.conv = all_conv;
             for (int k = 0; k < n_eig; ++k) {
                 out.vals.push_back(eig.vals[k]);
@@ -554,7 +693,8 @@ Ham* make_ham(int model, int nsites, const int* sector, int n_terms, const doubl
     int k = 0;
     for (int t = 0; t < n_terms; ++t) {
         Term term; term.coeff = cd(cre[t], cim[t]);
-        for (int f = 0; f < nfac[t]; ++f, ++k) term.factors.push_back({std::string(ops[k]), sites[k]});
+        for (int f = 0; f < nfac[t]; ++f, ++k)
+            term.factors.push_back({std::string(ops[k]), sites[k], op_id(model, std::string(ops[k]))});
         h->terms.push_back(term);
     }
     return h.release();
@@ -635,9 +775,14 @@ int qko_lanczos_from(void* hp, const double* v0, int maxiter, double tol, double
 
 int qko_davidson(void* hp, int n_eig, int max_sub, double tol, double* evals, double* evecs, int* iters, int* conv,
                  int* n_out) {
+    return qko_davidson_max(hp, n_eig, max_sub, tol, 100, evals, evecs, iters, conv, n_out);
+}
+
+int qko_davidson_max(void* hp, int n_eig, int max_sub, double tol, int max_iter, double* evals, double* evecs,
+                     int* iters, int* conv, int* n_out) {
     try {
         auto* h = static_cast<Ham*>(hp);
-        auto r = davidson(*h, n_eig, max_sub, tol);
+        auto r = davidson(*h, n_eig, max_sub, tol, max_iter);
         const uint64_t dim = h->basis.size();
         *iters = r.iters; *conv = r.conv ? 1 : 0; *n_out = (int)r.vals.size();
         for (size_t k = 0; k < r.vals.size(); ++k) {
@@ -753,6 +898,44 @@ void qko_rng_normal_complex(uint32_t seed, uint64_t n, double* out) {
     std::mt19937 rng(seed);
     std::normal_distribution<double> dist(0.0, 1.0);
     fill_complex(rng, dist, n, reinterpret_cast<cd*>(out));
+}
+
+void qko_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+void* qko_create_parallel(int model, int nsites, const int* sector, int n_terms, const double* cre, const double* cim,
+                          const int* nfac, const char* const* ops, const int* sites) {
+    try {
+        Ham* h = make_ham(model, nsites, sector, n_terms, cre, cim, nfac, ops, sites);
+        build_csr_parallel(*h);
+        return h;
+    } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+
+int qko_lanczos_timed(void* hp, const double* v0, int n_steps, double* step_seconds, int* n_done, double* energy) {
+    try {
+        auto* h = static_cast<Ham*>(hp);
+        const uint64_t dim = h->basis.size();
+        Vec v(dim);
+        if (v0) {
+            std::memcpy(v.data(), v0, dim * sizeof(cd));
+        } else {
+            std::mt19937 rng(1234);  // lanczos.cpp:115-120
+            std::uniform_real_distribution<double> dist(-1.0, 1.0);
+            fill_complex(rng, dist, dim, v.data());
+        }
+        std::vector<double> st;
+        auto r = lanczos(*h, v, n_steps, -1.0, &st);  // tol < 0: every step runs
+        *n_done = (int)st.size();
+        for (size_t i = 0; i < st.size(); ++i) step_seconds[i] = st[i];
+        *energy = r.energy;
+        return 0;
+    } catch (const std::exception& e) { g_err = e.what(); return -2; }
 }
 
 void* qko_sample_create(int model, int nsites, const int* sector, int n_terms, const double* cre, const double* cim,

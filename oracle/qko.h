@@ -43,6 +43,9 @@ int      qko_lanczos_from(void* h, const double* v0, int maxiter, double tol, do
                           int* conv, double* evec, double* alphas, double* betas);
 int      qko_davidson(void* h, int n_eig, int max_sub, double tol, double* evals, double* evecs, int* iters,
                       int* conv, int* n_out);
+/* qko_davidson with the iteration cap max_iter in place of the reference's 100. */
+int      qko_davidson_max(void* h, int n_eig, int max_sub, double tol, int max_iter, double* evals, double* evecs,
+                          int* iters, int* conv, int* n_out);
 int      qko_cf(void* h, const double* phi0, int n_iter, double* alphas, double* betas, double* norm,
                 int* n_alpha, int* n_beta);
 double   qko_spectral(const double* alphas, const double* betas, size_t n, double norm, double omega,
@@ -56,6 +59,20 @@ double   qko_tridiag_ground(const double* a, const double* b, int n, double* eve
  * reference binary built with g++ evaluates KComplex(dist(rng), dist(rng))). */
 void     qko_rng_uniform_complex(uint32_t seed, uint64_t n, double* out);
 void     qko_rng_normal_complex(uint32_t seed, uint64_t n, double* out);
+
+/* Host threads the oracle's OpenMP loops use from now on (n > 0). */
+void     qko_set_threads(int n);
+/* qko_create with the CSR of every row built by all host threads (same CSR,
+ * same entry order); for the CPU baseline at full size. */
+void*    qko_create_parallel(int model, int nsites, const int* sector, int n_terms, const double* coeff_re,
+                             const double* coeff_im, const int* nfac, const char* const* ops, const int* sites);
+/* The reference's Lanczos (full reorthogonalisation, tridiagonal ground state
+ * every step) for exactly n_steps steps, from v0 (interleaved complex, not
+ * normalised) or, with v0 NULL, from the reference's mt19937(1234) start
+ * vector; the wall time of every step is written to step_seconds[*n_done]
+ * (the Ritz vector at the end is not timed). */
+int      qko_lanczos_timed(void* h, const double* v0, int n_steps, double* step_seconds, int* n_done,
+                           double* energy);
 
 /* CPU baseline: the reference algorithm (host CSR + CSR gather + full
  * reorthogonalisation) timed on a bounded sample of rows.  Builds the CSR of

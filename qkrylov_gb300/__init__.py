@@ -114,6 +114,9 @@ _SIGS = {
     "qkrylov_lanczos_fixed_steps": (_i, [_vp, _i, _u64, _i, _dp, _c.POINTER(LanczosResultF64), _dp]),
     "qkrylov_kernel_launches": (_u64, []),
     "qkrylov_device_wait_timeouts": (_i, [_c.POINTER(_c.c_uint32)]),
+    "qkrylov_debug_inject_alloc_failure": (_i, [_c.c_int64]),
+    "qkrylov_debug_live_allocations": (_c.c_int64, []),
+    "qkrylov_debug_device_wait_probe": (_i, [_c.c_int64]),
     "qkrylov_vector_dot_device_f64": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_vector_dot_device_f32": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_vector_dot_device_f64_noalloc": (_i, [_vp, _vp, _u64, _dp, _vp]),
@@ -129,6 +132,7 @@ _SIGS = {
     "qkrylov_hamiltonian_entries": (_i, [_vp, _u64p, _u64p, _u64p, _dp]),
     "qkrylov_hamiltonian_select_kernel": (_i, [_vp, _i, _ip]),
     "qkrylov_hamiltonian_tuning": (_i, [_vp, _i, _ip, _dp]),
+    "qkrylov_hamiltonian_tuning_ex": (_i, [_vp, _i, _ip, _dp, _i]),
     "qkrylov_basis_states": (_i, [_vp, _u64, _u64, _u64p]),
     "qkrylov_davidson_lowest_ex": (_i, [_vp, _i, _i, _d, _i, _i, _dp, _dp, _dp, _vp, _dp]),
     "qkrylov_hamiltonian_benchmark_apply": (_i, [_vp, _i, _i, _dp]),
@@ -403,7 +407,8 @@ class MatrixFreeHamiltonian(_Handle):
         mode picks a kernel directly: 0 autotuned, 1 generic, 2 fast with one
         row per thread, 3 fast with shared-memory staging, 4 fast with four
         rows per thread, 5 four rows per thread staged, 6 four rows per thread
-        with a larger register budget.
+        with a larger register budget, 7 / 8 / 9 the tiled kernel over 1 / 2 /
+        4 outer blocks per CTA, 10 the class-persistent kernel.
         Returns whether the fast kernel is in use."""
         m = int(mode) if mode is not None else int(bool(generic))
         f = _c.c_int()
@@ -419,12 +424,13 @@ class MatrixFreeHamiltonian(_Handle):
 
     def tuning(self, fp32=True):
         """(variant, {variant: autotuned ms}) of the fast kernel used in mode 0;
-        variant names: "row", "staged", "rows4" ("generic" when it does not apply)."""
+        variant names: "row", "staged", "rows4", "rows4_staged", "rows4_wide",
+        "tile1", "tile2", "tile4", "class" ("generic" when it does not apply)."""
         v = _c.c_int()
-        ms = (_c.c_double * 5)()
-        _check(lib().qkrylov_hamiltonian_tuning(self._h, int(bool(fp32)), _c.byref(v), ms))
-        names = ["row", "staged", "rows4", "rows4_staged", "rows4_wide"]
-        return ("generic" if v.value < 0 else names[v.value]), {names[i]: ms[i] for i in range(5)}
+        names = ["row", "staged", "rows4", "rows4_staged", "rows4_wide", "tile1", "tile2", "tile4", "class"]
+        ms = (_c.c_double * len(names))()
+        _check(lib().qkrylov_hamiltonian_tuning_ex(self._h, int(bool(fp32)), _c.byref(v), ms, len(names)))
+        return ("generic" if v.value < 0 else names[v.value]), {names[i]: ms[i] for i in range(len(names))}
 
     def benchmark_apply(self, fp32=True, reps=10):
         """Mean CUDA-event duration (ms) of one apply of the selected kernel."""
@@ -485,14 +491,16 @@ def lanczos_ground_state(H, maxiter=200, tol=1e-12, v0=None, mixed=False, return
                          r.energy_tridiag, r)
 
 
-def lanczos_fixed_steps(H, n_steps, seed=0, mixed=True, v0=None, eigenvector_out=None):
+def lanczos_fixed_steps(H, n_steps, seed=0, mixed=True, v0=None, eigenvector_out=None, selective=False):
     """Exactly n_steps Lanczos steps (performance form).  v0 / eigenvector_out
-    are optional host arrays (complex128, reference order)."""
+    are optional host arrays (complex128, reference order).  mixed=False,
+    selective=True: FP64 with the mixed form's selective reorthogonalisation."""
     r = LanczosResultF64()
     n = H.dimension
     v0p = _dptr(_cvec(v0, n).view(_np.float64)) if v0 is not None else None
     evp = _dptr(eigenvector_out.view(_np.float64)) if eigenvector_out is not None else None
-    _check(lib().qkrylov_lanczos_fixed_steps(H._h, int(n_steps), int(seed), int(bool(mixed)), v0p, _c.byref(r), evp))
+    m = 1 if mixed else (2 if selective else 0)
+    _check(lib().qkrylov_lanczos_fixed_steps(H._h, int(n_steps), int(seed), m, v0p, _c.byref(r), evp))
     return r
 
 

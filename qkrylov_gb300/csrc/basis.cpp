@@ -337,12 +337,12 @@ struct Basis::DevCopy {
     ~DevCopy() {
         int cur = 0;
         if (cudaGetDevice(&cur) == cudaSuccess && cur != dev) cudaSetDevice(dev);
-        for (void* p : allocs) cudaFree(p);
+        for (void* p : allocs) device_free(p);
         if (cur != dev) cudaSetDevice(cur);
     }
     void* alloc(size_t bytes) {
         void* p = nullptr;
-        QKG_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 1)));
+        device_alloc(&p, std::max<size_t>(bytes, 1));
         allocs.push_back(p);
         return p;
     }
@@ -350,7 +350,7 @@ struct Basis::DevCopy {
     const T* upload(const std::vector<T>& v) {
         if (v.empty()) return nullptr;
         void* p = nullptr;
-        QKG_CUDA(cudaMalloc(&p, v.size() * sizeof(T)));
+        device_alloc(&p, v.size() * sizeof(T));
         allocs.push_back(p);
         QKG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
         return static_cast<const T*>(p);

@@ -444,7 +444,8 @@ template <class T, class A>
 class BlockEngine {
 public:
     using T2 = typename V2<T>::t;
-    BlockEngine(const std::vector<Hamiltonian*>& hs, int Rp, int Ruser) : hs_(hs), Rp_(Rp), Ruser_(Ruser) {
+    BlockEngine(const std::vector<Hamiltonian*>& hs, int Rp, int Ruser)
+        : hs_(hs), Rp_(Rp), Ruser_(Ruser), ws_lock_(hs[0]->workspace_lock()) {
         s_ = hs[0]->stream();
         std::vector<FastParams<A>> P(hs.size());
         std::vector<BItem> items;
@@ -563,6 +564,7 @@ public:
 private:
     std::vector<Hamiltonian*> hs_;
     int Rp_, Ruser_;
+    std::unique_lock<std::mutex> ws_lock_;  // the first Hamiltonian's workspace, held for the engine's life
     cudaStream_t s_ = nullptr;
     bool real_ = true, unif_ = true, oj_ = false;
     uint64_t rows_ = 0;

@@ -47,6 +47,24 @@ int guarded(F&& f) {
     }
 }
 
+// Solver calls run between two reads of the count of bounded device waits
+// that gave up (qkrylov_device_wait_timeouts).  A give-up during the call
+// makes its status QKRYLOV_ERROR_DEVICE_TIMEOUT; the kernel that gave up read
+// its operand from global memory instead, so the outputs are complete, but the
+// caller learns that a wait on an asynchronous copy ran out.
+void set_device(qkrylov_hamiltonian_h h);
+template <class F>
+int guarded_solve(qkrylov_hamiltonian_h h, F&& f) {
+    return guarded([&] {
+        set_device(h);  // the count belongs to the Hamiltonian's device
+        const uint32_t before = qkg::spmv_wait_timeouts();
+        f();
+        if (qkg::spmv_wait_timeouts() != before)
+            throw qkg::Error(qkg::DEVICE_TIMEOUT, "a bounded device wait gave up during this call (outputs computed "
+                                                  "from global memory)");
+    });
+}
+
 qkrylov_basis_h make_basis(qkg::Model m, int n, qkrylov_sector_h sector) {
     try {
         auto h = std::make_unique<qkrylov_basis_t>();
@@ -393,7 +411,7 @@ int qkrylov_hamiltonian_info(qkrylov_hamiltonian_h h, int* no, int* ni, int* nm,
 }
 
 int qkrylov_hamiltonian_select_kernel(qkrylov_hamiltonian_h h, int generic, int* fast_in_use) {
-    if (!h || !h->ptr || generic < 0 || generic > 6) return QKRYLOV_ERROR_INVALID_ARG;
+    if (!h || !h->ptr || generic < 0 || generic > qkg::Hamiltonian::kMaxMode) return QKRYLOV_ERROR_INVALID_ARG;
     h->ptr->set_kernel_mode(generic);
     if (fast_in_use) *fast_in_use = h->ptr->fast() ? 1 : 0;
     return QKRYLOV_SUCCESS;
@@ -403,8 +421,17 @@ int qkrylov_hamiltonian_tuning(qkrylov_hamiltonian_h h, int fp32, int* variant, 
     if (!h || !h->ptr || !variant) return QKRYLOV_ERROR_INVALID_ARG;
     const auto& H = *h->ptr;
     *variant = H.fast() ? (int)H.variant(fp32 ? 8 : 16) : -1;
+    if (*variant >= qkg::kFastVariantsV1) *variant = qkg::kFastVariantsV1;  // a variant this call does not list
     if (ms)
-        for (int v = 0; v < qkg::kFastVariants; ++v) ms[v] = H.tuned_ms(fp32 ? 0 : 1, v);
+        for (int v = 0; v < qkg::kFastVariantsV1; ++v) ms[v] = H.tuned_ms(fp32 ? 0 : 1, v);
+    return QKRYLOV_SUCCESS;
+}
+
+int qkrylov_hamiltonian_tuning_ex(qkrylov_hamiltonian_h h, int fp32, int* variant, double* ms, int n_ms) {
+    if (!h || !h->ptr || !variant || n_ms < 0 || (n_ms > 0 && !ms)) return QKRYLOV_ERROR_INVALID_ARG;
+    const auto& H = *h->ptr;
+    *variant = H.fast() ? (int)H.variant(fp32 ? 8 : 16) : -1;
+    for (int v = 0; v < n_ms; ++v) ms[v] = v < qkg::kFastVariants ? H.tuned_ms(fp32 ? 0 : 1, v) : 0.0;
     return QKRYLOV_SUCCESS;
 }
 
@@ -412,6 +439,7 @@ int qkrylov_hamiltonian_workspace(qkrylov_hamiltonian_h h, int release, uint64_t
     if (!h || !h->ptr) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         set_device(h);
+        const auto ws_lock = h->ptr->workspace_lock();
         if (release) h->ptr->release_workspace();
         if (bytes) *bytes = h->ptr->workspace_bytes();
     });
@@ -481,7 +509,7 @@ int qkrylov_lanczos_ground_state(qkrylov_hamiltonian_h h, int maxiter, float tol
 int qkrylov_lanczos_ground_state_complex(qkrylov_hamiltonian_h h, int maxiter, float tol, qkrylov_lanczos_result_c_t* r,
                                          float* ev) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         qkg::LanczosOpts o;
         o.maxiter = maxiter;
@@ -498,7 +526,7 @@ int qkrylov_lanczos_ground_state_complex(qkrylov_hamiltonian_h h, int maxiter, f
 int qkrylov_lanczos_ground_state_f64(qkrylov_hamiltonian_h h, int maxiter, double tol, const double* v0,
                                      qkrylov_lanczos_result_f64_t* r, double* ev) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         qkg::LanczosOpts o;
         o.maxiter = maxiter;
@@ -513,7 +541,7 @@ int qkrylov_lanczos_ground_state_f64(qkrylov_hamiltonian_h h, int maxiter, doubl
 int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, double tol, const double* v0,
                                        qkrylov_lanczos_result_f64_t* r, double* ev) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         qkg::LanczosOpts o;
         o.maxiter = maxiter;
@@ -527,18 +555,19 @@ int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, dou
 }
 int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed, const double* v0,
                                 qkrylov_lanczos_result_f64_t* r, double* ev) {
-    if (!h || !h->ptr || !r || n_steps <= 0) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    if (!h || !h->ptr || !r || n_steps <= 0 || mixed < 0 || mixed > 2) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded_solve(h, [&] {
         set_device(h);
         qkg::LanczosOpts o;
         o.maxiter = n_steps;
         o.fixed_steps = true;
+        o.selective = (mixed == 2);
         o.device_start = (v0 == nullptr);
         o.v0_ref = reinterpret_cast<const cd*>(v0);
         o.seed = seed;
         o.want_vec = ev != nullptr;
         o.evec_out = reinterpret_cast<cd*>(ev);
-        const auto res = mixed ? qkg::lanczos_mixed(*h->ptr, o) : qkg::lanczos_f64(*h->ptr, o);
+        const auto res = mixed == 1 ? qkg::lanczos_mixed(*h->ptr, o) : qkg::lanczos_f64(*h->ptr, o);
         fill_result(r, res);
     });
 }
@@ -553,6 +582,16 @@ int qkrylov_device_wait_timeouts(uint32_t* count) {
     if (*count) rc = QKRYLOV_ERROR_DEVICE_TIMEOUT;
     return rc;
 }
+int qkrylov_debug_inject_alloc_failure(int64_t after_n) {
+    qkg::inject_alloc_failure(after_n);
+    return QKRYLOV_SUCCESS;
+}
+int64_t qkrylov_debug_live_allocations(void) { return qkg::live_device_allocs(); }
+int qkrylov_debug_device_wait_probe(int64_t limit_ns) {
+    if (limit_ns <= 0) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] { qkg::tilek::wait_probe((long long)limit_ns); });
+}
+
 int qkrylov_set_device(int id) {
     return guarded([&] { QKG_CUDA(cudaSetDevice(id)); });
 }
@@ -563,7 +602,7 @@ int qkrylov_device_synchronize(void) {
 int qkrylov_davidson_lowest_complex(qkrylov_hamiltonian_h h, int n_eig, int max_sub, float tol, float* evals, float* evecs,
                                     qkrylov_davidson_result_c_t* info) {
     if (!h || !h->ptr || !evals || n_eig <= 0) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         const auto res = qkg::davidson_f64(*h->ptr, n_eig, max_sub, (double)tol, evecs != nullptr, true);
         const size_t k = std::min<size_t>((size_t)n_eig, res.evals.size());
@@ -582,7 +621,7 @@ int qkrylov_davidson_lowest_complex(qkrylov_hamiltonian_h h, int n_eig, int max_
 int qkrylov_davidson_lowest_complex_f64(qkrylov_hamiltonian_h h, int n_eig, int max_sub, double tol, double* evals,
                                         double* evecs, qkrylov_davidson_result_c_t* info) {
     if (!h || !h->ptr || !evals || n_eig <= 0) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         const auto res = qkg::davidson_f64(*h->ptr, n_eig, max_sub, tol, evecs != nullptr);
         const size_t k = std::min<size_t>((size_t)n_eig, res.evals.size());
@@ -599,7 +638,7 @@ int qkrylov_davidson_lowest_ex(qkrylov_hamiltonian_h h, int n_eig, int max_sub, 
                                double* evals, double* evecs, double* residuals, qkrylov_davidson_result_c_t* info,
                                double* seconds) {
     if (!h || !h->ptr || !evals || n_eig <= 0 || max_iter < 1 || max_iter > 100) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         const auto res = mixed ? qkg::davidson_mixed(*h->ptr, n_eig, max_sub, tol, evecs != nullptr, max_iter)
                                : qkg::davidson_f64(*h->ptr, n_eig, max_sub, tol, evecs != nullptr, false, max_iter);
@@ -619,7 +658,7 @@ int qkrylov_davidson_lowest_ex(qkrylov_hamiltonian_h h, int n_eig, int max_sub, 
 int qkrylov_continued_fraction_coeffs_complex(qkrylov_hamiltonian_h h, const float* phi0, int n_iter, float* alphas,
                                               float* betas, float* norm, int* num) {
     if (!h || !h->ptr || !phi0 || !alphas || !betas || !norm || n_iter <= 0) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         const uint64_t n = h->ptr->dim();
         std::vector<cd> p(n);
@@ -634,7 +673,7 @@ int qkrylov_continued_fraction_coeffs_complex(qkrylov_hamiltonian_h h, const flo
 int qkrylov_continued_fraction_coeffs_complex_f64(qkrylov_hamiltonian_h h, const double* phi0, int n_iter, double* alphas,
                                                   double* betas, double* norm, int* num, int* num_betas) {
     if (!h || !h->ptr || !phi0 || !alphas || !betas || !norm || n_iter <= 0) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         const auto res = qkg::cf_f64(*h->ptr, reinterpret_cast<const cd*>(phi0), n_iter);
         *norm = res.norm;
@@ -670,7 +709,7 @@ int qkrylov_evaluate_spectral_grid_f64(const double* alphas, const double* betas
 
 int qkrylov_ftlm(qkrylov_hamiltonian_h h, float beta, int n_random, int n_steps, qkrylov_ftlm_result_c_t* r) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         r->beta = beta;
         r->partition_function = r->internal_energy = r->specific_heat = 0.0f;
@@ -687,7 +726,7 @@ int qkrylov_ftlm(qkrylov_hamiltonian_h h, float beta, int n_random, int n_steps,
 }
 int qkrylov_ftlm_f64(qkrylov_hamiltonian_h h, double beta, int n_random, int n_steps, qkrylov_ftlm_result_f64_t* r) {
     if (!h || !h->ptr || !r) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         r->beta = beta;
         r->partition_function = r->internal_energy = r->specific_heat = 0.0;
@@ -703,7 +742,7 @@ int qkrylov_ftlm_f64(qkrylov_hamiltonian_h h, double beta, int n_random, int n_s
 int qkrylov_ftlm_multi_beta_f64(qkrylov_hamiltonian_h h, const double* betas, int n_beta, int n_random, int n_steps,
                                 double* Z, double* E, double* Cv, double* log_shift) {
     if (!h || !h->ptr || !betas || n_beta < 0 || !Z || !E || !Cv) return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(h, [&] {
         set_device(h);
         const auto tri = qkg::ftlm_tridiags_f64(*h->ptr, n_random, n_steps);
         qkg::ftlm_observables(tri, betas, n_beta, Z, E, Cv, log_shift != nullptr, log_shift);
@@ -760,7 +799,7 @@ int qkrylov_block_lanczos_tridiag(const qkrylov_hamiltonian_h* hams, int n_ham, 
         !n_beta || !norm2 || (start_kind == QKRYLOV_START_GIVEN && !start_vectors) ||
         (vectors_per_lane != 0 && vectors_per_lane != 1 && vectors_per_lane != 2 && vectors_per_lane != 4))
         return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(hams[0], [&] {
         set_device(hams[0]);
         qkg::BlockOpts o = block_opts(n_vec, n_steps, mixed, start_kind, seed);
         o.vpl = vectors_per_lane;
@@ -794,7 +833,7 @@ int qkrylov_ftlm_sectors_f64(const qkrylov_hamiltonian_h* hams, int n_ham, const
     if (!collect_hams(hams, n_ham, hs) || !betas || n_beta < 0 || n_random < 1 || n_random > 32 || n_steps < 0 ||
         !Z || !E || !Cv || start_kind == QKRYLOV_START_GIVEN)
         return QKRYLOV_ERROR_INVALID_ARG;
-    return guarded([&] {
+    return guarded_solve(hams[0], [&] {
         set_device(hams[0]);
         const qkg::BlockTridiag t = qkg::block_lanczos(hs, block_opts(n_random, n_steps, mixed, start_kind, seed));
         qkg::ftlm_observables_block(t, betas, n_beta, Z, E, Cv, log_shift != nullptr, log_shift);

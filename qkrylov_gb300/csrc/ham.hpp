@@ -7,6 +7,7 @@
 
 #include <complex>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 namespace qkg {
@@ -31,13 +32,26 @@ enum DiagMode : int { DIAG_U8 = 0, DIAG_U16 = 1, DIAG_FULL = 2 };
 
 // Fast SpMV kernel variants: one row per thread, the outer block's slice of x
 // staged in shared memory, four rows per thread, four rows per thread with the
-// block staged, four rows per thread with a larger register budget.
-enum FastVariant : int { FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3, FV_ROWS4_WIDE = 4 };
-constexpr int kFastVariants = 5;
+// block staged, four rows per thread with a larger register budget, the
+// tiled kernel over 1, 2 or 4 outer blocks per CTA, and the class-persistent
+// kernel (spmv_tile.cu).
+enum FastVariant : int {
+    FV_ROW = 0, FV_STAGED = 1, FV_ROWS4 = 2, FV_ROWS4_STAGED = 3, FV_ROWS4_WIDE = 4,
+    FV_TILE1 = 5, FV_TILE2 = 6, FV_TILE4 = 7, FV_CLASS = 8
+};
+constexpr int kFastVariants = 9;
+constexpr int kFastVariantsV1 = 5;  // variants reported by qkrylov_hamiltonian_tuning
+inline int tile_g(FastVariant v) { return v == FV_TILE1 ? 1 : v == FV_TILE2 ? 2 : v == FV_TILE4 ? 4 : 0; }
+inline int tile_index(int g) { return g == 1 ? 0 : g == 2 ? 1 : 2; }
 
 // Bounded device waits of the SpMV kernels that gave up on the current GPU
 // (waits for the GPU first).
 uint32_t spmv_wait_timeouts();
+namespace tilek {
+// Test hook: one bounded wait (limit_ns of global time, clamped to 1 us .. 1 s)
+// on an mbarrier that nothing completes, counted as a give-up.
+void wait_probe(long long limit_ns);
+}  // namespace tilek
 
 // Device-resident Lanczos step.  The operands of one Lanczos-mode SpMV are kept
 // in device memory and rewritten by the step's last kernel for the next step:
@@ -113,21 +127,47 @@ public:
     // kernel mode: 0 automatic (autotuned), 1 generic kernel, 2 fast kernel
     // one row per thread, 3 fast kernel with shared-memory staging, 4 fast
     // kernel four rows per thread, 5 four rows per thread with staging, 6 four
-    // rows per thread with the larger register budget
+    // rows per thread with the larger register budget, 7 / 8 / 9 the tiled
+    // kernel over 1 / 2 / 4 outer blocks per CTA, 10 the class-persistent kernel
+    static constexpr int kMaxMode = 10;
     void set_kernel_mode(int m) { mode_ = m; force_generic_ = (m == 1); }
     void force_generic(bool on) { set_kernel_mode(on ? 1 : 0); }
     // fast-kernel variant for vectors of elem_bytes per element
     // dynamic shared memory of a staged variant: the largest outer block's slice
     // of x plus one element on either side (the copy starts on a 16-byte boundary)
     size_t stage_bytes(size_t elem_bytes) const { return ((max_block_ + 2) * elem_bytes + 15) / 16 * 16; }
+    // the tiled kernel over G blocks per CTA fits its shared memory
+    bool can_tile(int G, size_t elem_bytes) const;
+    size_t tile_smem_bytes(int G, size_t elem_bytes) const;
+    uint32_t tile_slot_elems(size_t elem_bytes) const;
+    const void* tile_items(int G) const { return tile_items_[tile_index(G)].p; }
+    // class-persistent kernel: its shared memory fits; its plan (device
+    // pointers), shared memory and grid (one CTA per SM, at most one per block)
+    bool can_class(size_t elem_bytes) const;
+    size_t class_smem_bytes(size_t elem_bytes) const;
+    unsigned class_grid() const { return class_grid_; }
+    const void* class_blocks() const { return class_blocks_.p; }  // tilek::CBlock
+    const void* class_info() const { return class_info_.p; }      // tilek::CClass
+    uint32_t class_nblocks() const { return class_nblocks_; }
+    uint32_t class_ell_cap() const { return class_ell_cap_; }
+    uint32_t class_gcap() const { return class_gcap_; }
+    uint32_t class_maxw() const { return class_maxw_; }
+    size_t n_tile_items(int G) const { return n_tile_[tile_index(G)]; }
     FastVariant variant(size_t elem_bytes) const {
         const bool can_stage = max_block_ > 0 && stage_bytes(elem_bytes) <= kStageLimit;
+        if (mode_ >= 7 && mode_ <= 9) {
+            const FastVariant t = (FastVariant)(FV_TILE1 + (mode_ - 7));
+            return can_tile(tile_g(t), elem_bytes) ? t : FV_ROWS4;
+        }
+        if (mode_ == 10) return can_class(elem_bytes) ? FV_CLASS : FV_ROWS4;
         if (mode_ == 2) return FV_ROW;
         if (mode_ == 3) return can_stage ? FV_STAGED : FV_ROW;
         if (mode_ == 4) return FV_ROWS4;
         if (mode_ == 5) return can_stage ? FV_ROWS4_STAGED : FV_ROWS4;
         if (mode_ == 6) return FV_ROWS4_WIDE;
         const FastVariant v = pref_[elem_bytes == 16 ? 1 : 0];
+        if (tile_g(v) && !can_tile(tile_g(v), elem_bytes)) return FV_ROWS4;
+        if (v == FV_CLASS && !can_class(elem_bytes)) return FV_ROWS4;
         if (v == FV_STAGED && !can_stage) return FV_ROW;
         if (v == FV_ROWS4_STAGED && !can_stage) return FV_ROWS4;
         return v;
@@ -152,9 +192,13 @@ public:
     // space of the device-resident Lanczos, tens of GB): cudaFree of 64 GB
     // takes about 25 ms, a tenth of a 200-step run.  Grows on demand, contents
     // undefined; released with the Hamiltonian or by release_workspace().
+    // A solver that uses the workspace holds workspace_lock() for the whole
+    // call, so two calls on one Hamiltonian from different host threads take
+    // turns instead of freeing each other's Krylov space.
     DBuf& krylov_workspace(size_t bytes) const;
     void release_workspace() const { kws_.reset(); }
     size_t workspace_bytes() const { return kws_.bytes; }
+    std::unique_lock<std::mutex> workspace_lock() const { return std::unique_lock<std::mutex>(kws_mu_); }
 
 private:
     void build_diagonal();
@@ -176,6 +220,11 @@ private:
     double tune_ms_[2][kFastVariants] = {};
     DBuf items_blk_;            // one work item per outer block (staged kernel)
     size_t n_items_blk_ = 0, max_block_ = 0;
+    DBuf class_blocks_, class_info_;  // class-persistent kernel: sorted blocks, per-class table ranges
+    uint32_t class_nblocks_ = 0, class_ell_cap_ = 0, class_gcap_ = 0, class_maxw_ = 0;
+    unsigned class_grid_ = 0;
+    DBuf tile_items_[3];        // tiled kernel: groups of 1, 2, 4 outer blocks
+    size_t n_tile_[3] = {0, 0, 0};
     double u_ar_ = 0.0, u_ai_ = 0.0;
     int rbits_ = 0;
     size_t n_ient_ = 0;
@@ -198,6 +247,7 @@ private:
     DBuf dcode_, dtab64_, dtab32_, dfull64_, dfull32_;
     int n_dtab_ = 0;
     mutable DBuf kws_;
+    mutable std::mutex kws_mu_;
 };
 
 // ------------------------------------------------------------ Krylov algebra

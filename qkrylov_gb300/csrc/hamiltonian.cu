@@ -24,23 +24,49 @@
 //            same block, rank = block offset + inner_rank[b'];
 //   mixed  - everything else: full rank of the target.
 #include "fast_common.cuh"
+#include "tile.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <string>
 #include <cstring>
 #include <set>
 #include <utility>
 
 namespace qkg {
 
+namespace {
+std::atomic<int64_t> g_live_allocs{0};
+std::atomic<int64_t> g_fail_after{-1};  // allocations left before an injected failure (-1: none)
+}  // namespace
+
+void device_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    int64_t left = g_fail_after.load();
+    while (left >= 0 && !g_fail_after.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left == 0)
+        throw Error(CUDA_ERR, "cudaMalloc(" + std::to_string(bytes) + " bytes): out of memory (injected failure)");
+    QKG_CUDA(cudaMalloc(p, std::max<size_t>(bytes, 1)));
+    ++g_live_allocs;
+}
+void device_free(void* p) {
+    if (!p) return;
+    cudaFree(p);
+    --g_live_allocs;
+}
+int64_t live_device_allocs() { return g_live_allocs.load(); }
+void inject_alloc_failure(int64_t after_n) { g_fail_after.store(after_n < 0 ? -1 : after_n); }
+
 void DBuf::alloc(size_t n) {
     reset();
     if (n) {
-        QKG_CUDA(cudaMalloc(&p, n));
+        device_alloc(&p, n);
         bytes = n;
     }
 }
 void DBuf::reset() {
-    if (p) cudaFree(p);
+    device_free(p);
     p = nullptr;
     bytes = 0;
 }
@@ -416,11 +442,13 @@ static_assert(kRowsPerThread * kBlock == kChunk, "work items hold kRowsPerThread
 #ifndef QKG_STAGE_BULK
 #define QKG_STAGE_BULK 1
 #endif
-// Waits on an mbarrier that gave up (bounded spin): counted here, read by the
-// host through spmv_wait_timeouts(); the kernel then computes on whatever the
-// copy delivered, so a non-zero count means the results of that launch are void.
+// Waits on an mbarrier that gave up (bounded by the global timer): counted
+// here, read by the host through spmv_wait_timeouts().  A thread whose wait
+// gave up reads x from global memory instead of the staged copy (its results
+// stay valid) and, before the CTA exits, waits once more (bounded) for the copy
+// still in flight into its shared memory.
 __device__ unsigned int g_spmv_wait_timeouts;
-constexpr uint32_t kMbarSpinLimit = 1u << 24;  // about a second of polling
+constexpr unsigned long long kMbarWaitNs = 2000000000ull;  // 2 s of global time
 
 // One-shot bulk copy of `bytes` (a multiple of 16, both addresses 16-byte
 // aligned) from global to shared memory, completing on the mbarrier `bar`.
@@ -436,10 +464,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                  "l"(src), "r"(bytes), "r"(b)
                  : "memory");
 }
-// Bounded wait for phase 0 of `bar`; false if the limit was reached.
-__device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
+// Bounded wait for phase 0 of `bar`; false once limit_ns of global time passed.
+__device__ __noinline__ bool mbar_wait0(unsigned long long* bar, unsigned long long limit_ns) {
     const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar);
-    for (uint32_t i = 0; i < kMbarSpinLimit; ++i) {
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (;;) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
@@ -447,8 +477,10 @@ __device__ __forceinline__ bool mbar_wait0(unsigned long long* bar) {
             : "r"(b)
             : "memory");
         if (done) return true;
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) return false;
     }
-    return false;
 }
 
 #ifndef QKG_ROWS_MINB_WIDE
@@ -523,6 +555,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     const uint32_t rmask = (1u << p.rbits) - 1u;
 
     A dot_hi = 0, dot_lo = 0;
+    bool staged_ok = true;  // STAGE: the slice is read from shared memory
     // a warp covers RT * 32 consecutive rows: row q of this thread is tbase + 32 q
     const uint32_t tbase = (threadIdx.x & ~31u) * RT + (threadIdx.x & 31u);
     // passes of kChunk rows (one pass unless a whole outer block is staged)
@@ -564,9 +597,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
     }
     // the four rows' ELL walks, slot by slot
 #if QKG_STAGE_BULK
-    if (STAGE && bulk && pass == 0 && !mbar_wait0(&s_bar)) {
+    if (STAGE && bulk && pass == 0 && !mbar_wait0(&s_bar, kMbarWaitNs)) {
         atomicAdd(&g_spmv_wait_timeouts, 1u);
-        mbar_wait0(&s_bar);  // the copy may still be writing shared memory: wait once more
+        staged_ok = false;
     }
 #endif
 #if QKG_ELL_PREFETCH
@@ -582,7 +615,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         for (int q = 0; q < RT; ++q) {
             e0[q] += 32;
             nxt[q] = (cur[q] != kEllEmpty && e0[q] < e1[q]) ? __ldg(p.ient + e0[q]) : kEllEmpty;
-            if (cur[q] != kEllEmpty) xv[q] = STAGE ? xst[cur[q] & rmask] : x[block_off + (cur[q] & rmask)];
+            if (cur[q] != kEllEmpty)
+                xv[q] = (STAGE && staged_ok) ? xst[cur[q] & rmask] : x[block_off + (cur[q] & rmask)];
         }
         more = false;
 #pragma unroll
@@ -617,7 +651,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         T2 xv[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q)
-            if (ent[q] != kEllEmpty) xv[q] = STAGE ? xst[ent[q] & rmask] : x[block_off + (ent[q] & rmask)];
+            if (ent[q] != kEllEmpty)
+                xv[q] = (STAGE && staged_ok) ? xst[ent[q] & rmask] : x[block_off + (ent[q] & rmask)];
 #pragma unroll
         for (int q = 0; q < RT; ++q) {
             if (ent[q] == kEllEmpty) {
@@ -679,7 +714,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         const uint32_t row = (uint32_t)it.row0 + rl;
         dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
                                        : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
-        xd[q] = STAGE ? xst[rl] : x[row];
+        xd[q] = (STAGE && staged_ok) ? xst[rl] : x[row];
         if (vprev) pv[q] = vprev[row];
     }
 #pragma unroll
@@ -708,6 +743,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         }
     }
     }
+#if QKG_STAGE_BULK
+    // a copy that outlived this thread's wait is still writing shared memory:
+    // wait for it (bounded) before the CTA exits
+    if (STAGE && bulk && !staged_ok && !mbar_wait0(&s_bar, kMbarWaitNs)) atomicAdd(&g_spmv_wait_timeouts, 1u);
+#endif
     if (p.apart) {
         if (sizeof(A) == 4) {
             const float2 t = block_sum_ff((float)dot_hi, (float)dot_lo);
@@ -1094,9 +1134,92 @@ void Hamiltonian::build_fast() {
     for (const auto& w : bitems) max_block_ = std::max<size_t>(max_block_, w.count);
     n_items_blk_ = bitems.size();
     upload_vec(items_blk_, bitems);
+    // Tiled kernel: the blocks of each inner class in launch order (the pair
+    // order above), cut into groups of G; the groups of all classes run in the
+    // order of their first block, so blocks joined by a straddling term run
+    // side by side.
+    {
+        auto key = [&](uint32_t a) -> uint64_t {
+            if (pair_bit < 0) return a;
+            const uint32_t m = 1u << pair_bit;
+            return ((uint64_t)(a & ~m) << 1) | ((a & m) ? 1u : 0u);
+        };
+        std::vector<std::pair<uint32_t, std::vector<WorkItem>>> classes;  // (inner_base, blocks)
+        for (const auto& w : bitems) {
+            size_t c = 0;
+            while (c < classes.size() && classes[c].first != w.inner_base) ++c;
+            if (c == classes.size()) classes.push_back({w.inner_base, {}});
+            classes[c].second.push_back(w);
+        }
+        for (int gi = 0; gi < 3; ++gi) {
+            const int G = gi == 0 ? 1 : gi == 1 ? 2 : 4;
+            std::vector<std::pair<uint64_t, tilek::TileItem>> groups;
+            for (const auto& cl : classes) {
+                const auto& v = cl.second;
+                for (size_t i = 0; i < v.size(); i += G) {
+                    tilek::TileItem t{};
+                    t.nblk = (uint32_t)std::min<size_t>(G, v.size() - i);
+                    for (uint32_t k = 0; k < t.nblk; ++k) t.a[k] = v[i + k].a;
+                    for (uint32_t k = t.nblk; k < (uint32_t)tilek::kMaxG; ++k) t.a[k] = v[i].a;
+                    t.width = v[i].count;
+                    t.inner_base = v[i].inner_base;
+                    t.grp = v[i].pad;
+                    groups.push_back({key(v[i].a), t});
+                }
+            }
+            std::stable_sort(groups.begin(), groups.end(),
+                             [](const auto& x, const auto& y) { return x.first < y.first; });
+            std::vector<tilek::TileItem> tv;
+            tv.reserve(groups.size());
+            for (const auto& g : groups) tv.push_back(g.second);
+            n_tile_[gi] = tv.size();
+            upload_vec(tile_items_[gi], tv);
+        }
+        // Class-persistent kernel: the blocks sorted by inner class (classes of
+        // more outer bits first), in launch order inside a class; per class its
+        // width, inner_state base, inner-table groups and their entry range.
+        std::vector<tilek::CClass> cinfo;
+        std::vector<std::pair<uint64_t, tilek::CBlock>> cblk;
+        class_maxw_ = class_ell_cap_ = class_gcap_ = 0;
+        for (size_t c = 0; c < classes.size(); ++c) {
+            const WorkItem& w0 = classes[c].second.front();
+            tilek::CClass cc;
+            cc.W = w0.count;
+            cc.inner_base = w0.inner_base;
+            cc.gbase = w0.pad;
+            cc.ngroups = (w0.count + 31) / 32;
+            cc.ell0 = gptr[cc.gbase];
+            cc.ell1 = gptr[cc.gbase + cc.ngroups];
+            cinfo.push_back(cc);
+            class_maxw_ = std::max(class_maxw_, cc.W);
+            class_ell_cap_ = std::max(class_ell_cap_, cc.ell1 - cc.ell0);
+            class_gcap_ = std::max(class_gcap_, cc.ngroups);
+            const int ic = B.inner_all ? 0 : B.inner_class_of(w0.a);
+            for (const auto& w : classes[c].second)
+                cblk.push_back({((uint64_t)(uint32_t)(64 - ic) << 40) | key(w.a), tilek::CBlock{w.a, (uint32_t)c}});
+        }
+        std::stable_sort(cblk.begin(), cblk.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+        std::vector<tilek::CBlock> cb;
+        for (const auto& e : cblk) cb.push_back(e.second);
+        class_nblocks_ = (uint32_t)cb.size();
+        upload_vec(class_blocks_, cb);
+        upload_vec(class_info_, cinfo);
+        int sms = 0;
+        QKG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_));
+        class_grid_ = (unsigned)std::min<uint64_t>((uint64_t)std::max(sms, 1), class_nblocks_);
+    }
     if (stage_bytes(8) <= kStageLimit) allow_stage_smem<float, float>(stage_bytes(8));
     if (stage_bytes(16) <= kStageLimit) allow_stage_smem<double, double>(stage_bytes(16));
     fast_ = true;
+    {
+        size_t t32 = 0, t64 = 0;
+        for (int G : {1, 2, 4}) {
+            if (can_tile(G, 8)) t32 = std::max(t32, tile_smem_bytes(G, 8));
+            if (can_tile(G, 16)) t64 = std::max(t64, tile_smem_bytes(G, 16));
+        }
+        if (t32) tilek::tile_allow_smem<float, float>(t32);
+        if (t64) tilek::tile_allow_smem<double, double>(t64);
+    }
     autotune();
 }
 
@@ -1116,7 +1239,9 @@ void Hamiltonian::autotune() {
         double best = 0.0;
         for (int v = 0; v < kFastVariants; ++v) {
             if ((v == FV_STAGED || v == FV_ROWS4_STAGED) && !(stage_bytes(e) <= kStageLimit)) continue;
-            mode_ = 2 + v;  // modes 2..6 select variants 0..4
+            if (tile_g((FastVariant)v) && !can_tile(tile_g((FastVariant)v), e)) continue;
+            if (v == FV_CLASS && !can_class(e)) continue;
+            mode_ = 2 + v;  // modes 2..10 select variants 0..8
             auto run = [&] {
                 if (prec) apply_f64(x.as<double2>(), y.as<double2>(), stream_);
                 else apply_f32(x.as<float2>(), y.as<float2>(), stream_);
@@ -1268,7 +1393,55 @@ uint32_t spmv_wait_timeouts() {
     QKG_CUDA(cudaDeviceSynchronize());
     uint32_t c = 0;
     QKG_CUDA(cudaMemcpyFromSymbol(&c, g_spmv_wait_timeouts, sizeof(c)));
-    return c;
+    return c + tilek::tile_wait_timeouts();
+}
+
+uint32_t Hamiltonian::tile_slot_elems(size_t elem_bytes) const { return tilek::tile_slot(max_block_, elem_bytes); }
+size_t Hamiltonian::tile_smem_bytes(int G, size_t elem_bytes) const {
+    const FastSet& fs = elem_bytes == 16 ? f64s_ : f32s_;
+    return tilek::tile_smem(G, elem_bytes, tile_slot_elems(elem_bytes), fs.n_inner, unif_, elem_bytes / 2);
+}
+bool Hamiltonian::can_tile(int G, size_t elem_bytes) const {
+    return fast_ && max_block_ > 0 && n_tile_[tile_index(G)] > 0 &&
+           tile_smem_bytes(G, elem_bytes) <= tilek::kTileSmemLimit;
+}
+
+size_t Hamiltonian::class_smem_bytes(size_t elem_bytes) const {
+    const FastSet& fs = elem_bytes == 16 ? f64s_ : f32s_;
+    tilek::ClassPlan c{};
+    c.slot = tilek::tile_slot(class_maxw_, elem_bytes);
+    c.ell_cap = class_ell_cap_;
+    c.gcap = class_gcap_;
+    return tilek::class_smem(c, elem_bytes, fs.n_inner, unif_, elem_bytes / 2);
+}
+bool Hamiltonian::can_class(size_t elem_bytes) const {
+    return fast_ && class_nblocks_ > 0 && class_maxw_ <= (uint32_t)(tilek::kClassThreads * tilek::kClassCols) &&
+           class_smem_bytes(elem_bytes) <= tilek::kTileSmemLimit;
+}
+
+// Launch the class-persistent variant.
+template <class T, class A>
+static void launch_class_variant(const Hamiltonian& H, const FastParams<A>& p, bool real, bool unif,
+                                 const typename V2<T>::t* x, typename V2<T>::t* y, cudaStream_t s) {
+    const size_t e = sizeof(typename V2<T>::t);
+    tilek::ClassPlan c;
+    c.blocks = static_cast<const tilek::CBlock*>(H.class_blocks());
+    c.classes = static_cast<const tilek::CClass*>(H.class_info());
+    c.nblocks = H.class_nblocks();
+    c.slot = tilek::tile_slot(H.class_maxw(), e);
+    c.ell_cap = H.class_ell_cap();
+    c.gcap = H.class_gcap();
+    tilek::launch_class<T, A>(p, c, H.class_grid(), real, unif, x, y, H.class_smem_bytes(e), s);
+}
+
+// Launch a tiled variant on the Hamiltonian's group list for it.
+template <class T, class A>
+static void launch_tile_variant(const Hamiltonian& H, const FastParams<A>& p, FastVariant v, bool real, bool unif,
+                                const typename V2<T>::t* x, typename V2<T>::t* y, cudaStream_t s) {
+    const int G = tile_g(v);
+    const size_t e = sizeof(typename V2<T>::t);
+    tilek::launch_tile<T, A>(p, static_cast<const tilek::TileItem*>(H.tile_items(G)), H.n_tile_items(G), G, real,
+                             unif, x, y, H.tile_slot_elems(e), H.tile_smem_bytes(G, e), s);
 }
 
 DBuf& Hamiltonian::krylov_workspace(size_t bytes) const {
@@ -1493,6 +1666,13 @@ static void launch_spmv(const DevBasis& b, const TermSet& ts, const DBuf& items,
 void Hamiltonian::apply_f64(const double2* x, double2* y, cudaStream_t s) const {
     if (fast()) {
         const FastVariant v = variant(16);
+        if (tile_g(v) || v == FV_CLASS) {
+            FastParams<double> p;
+            fast_params(p);
+            if (v == FV_CLASS) launch_class_variant<double, double>(*this, p, all_real_, unif_, x, y, s);
+            else launch_tile_variant<double, double>(*this, p, v, all_real_, unif_, x, y, s);
+            return;
+        }
         const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
         FastParams<double> p;
         fast_params(p);
@@ -1514,15 +1694,25 @@ void Hamiltonian::apply_lanczos_f32(const LanczosHooks& lz, cudaStream_t s) cons
     const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
     FastParams<float> p;
     fast_params(p);
-    size_t ni = 0;
-    p.items = items_of(v, &ni);
     p.lz = lz.op;
     p.apart = lz.apart;
+    if (v == FV_CLASS) {
+        launch_class_variant<float, float>(*this, p, all_real_, unif_, nullptr, nullptr, s);
+        return;
+    }
+    if (tile_g(v)) {
+        launch_tile_variant<float, float>(*this, p, v, all_real_, unif_, nullptr, nullptr, s);
+        return;
+    }
+    size_t ni = 0;
+    p.items = items_of(v, &ni);
     launch_fast<float, float>(p, ni, all_real_, unif_, nullptr, nullptr, s, v, st ? stage_bytes(8) : 0);
 }
 
 size_t Hamiltonian::lanczos_parts() const {
     if (!fast()) return n_items_;
+    if (variant(8) == FV_CLASS) return class_grid_;
+    if (tile_g(variant(8))) return n_tile_items(tile_g(variant(8)));
     size_t ni = 0;
     items_of(variant(8), &ni);
     return ni;
@@ -1540,6 +1730,13 @@ const WorkItem* Hamiltonian::items_of(FastVariant v, size_t* n) const {
 void Hamiltonian::apply_f32(const float2* x, float2* y, cudaStream_t s) const {
     if (fast()) {
         const FastVariant v = variant(8);
+        if (tile_g(v) || v == FV_CLASS) {
+            FastParams<float> p;
+            fast_params(p);
+            if (v == FV_CLASS) launch_class_variant<float, float>(*this, p, all_real_, unif_, x, y, s);
+            else launch_tile_variant<float, float>(*this, p, v, all_real_, unif_, x, y, s);
+            return;
+        }
         const bool st = v == FV_STAGED || v == FV_ROWS4_STAGED;
         FastParams<float> p;
         fast_params(p);

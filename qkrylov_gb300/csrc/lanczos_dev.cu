@@ -254,6 +254,7 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     LanczosOut out;
     const uint64_t n = H.dim();
     if (n == 0) return out;
+    const auto ws_lock = H.workspace_lock();
     cudaStream_t st = H.stream();
     const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
     if (nmax <= 0) return out;

@@ -22,8 +22,12 @@
 //    partial slot it reads and the result slot before reading them.
 //
 // The first call on a GPU looks up the array's device address there
-// (cudaGetSymbolAddress, with that GPU current) and caches it; that first
-// call should come before any stream capture.
+// (cudaGetSymbolAddress, with that GPU current), caches it, and makes sure both
+// kernels are loaded on that GPU.  With CUDA's lazy module loading that first
+// call is when the array and the kernels' code take their device memory, so a
+// call with n = 0 serves as the warm-up a caller makes before it reserves the
+// GPU's memory for itself.  The call waits for its stream (it reads the result
+// back to the host), so it cannot be used inside a stream capture.
 #include "../../include/qkrylov_c_api.h"
 #include "qkg.hpp"
 
@@ -92,7 +96,8 @@ __global__ void __launch_bounds__(kNoAllocThreads) na_finish_kernel(double2* __r
 std::mutex g_na_mu;
 double2* g_na_addr[kMaxDevices] = {};
 
-// Device address of the scratch array on the current GPU (looked up once per GPU).
+// Device address of the scratch array on the current GPU (looked up once per
+// GPU, when both kernels are also loaded there).
 double2* na_scratch_on_current_device() {
     int dev = -1;
     QKG_CUDA(cudaGetDevice(&dev));
@@ -104,6 +109,9 @@ double2* na_scratch_on_current_device() {
         if (e != cudaSuccess || !p)
             throw qkg::Error(qkg::CUDA_ERR, std::string("cudaGetSymbolAddress(g_noalloc_dot_scratch): ") +
                                                  cudaGetErrorString(e));
+        cudaFuncAttributes fa;
+        QKG_CUDA(cudaFuncGetAttributes(&fa, na_partial_kernel));
+        QKG_CUDA(cudaFuncGetAttributes(&fa, na_finish_kernel));
         g_na_addr[dev] = static_cast<double2*>(p);
     }
     return g_na_addr[dev];
@@ -123,8 +131,8 @@ extern "C" int qkrylov_vector_dot_device_f64_noalloc(const void* d_x, const void
     try {
         qkg::set_last_error("");
         result[0] = result[1] = 0.0;
+        double2* scratch = na_scratch_on_current_device();  // n = 0: the warm-up only
         if (!n) return QKRYLOV_SUCCESS;
-        double2* scratch = na_scratch_on_current_device();
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         const int nblocks = (int)((n + kNoAllocPerBlock - 1) / kNoAllocPerBlock);
         na_partial_kernel<<<nblocks, kNoAllocThreads, 0, s>>>(static_cast<const double2*>(d_x),

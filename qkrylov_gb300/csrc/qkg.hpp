@@ -46,6 +46,14 @@ void add_launches(int64_t d);
         ::qkg::count_launch();       \
         QKG_CUDA(cudaGetLastError()); \
     } while (0)
+// Device memory of the library goes through device_alloc/device_free: they
+// count the live allocations (qkrylov_debug_live_allocations) and let a test
+// make the n-th allocation fail as cudaMalloc would on an exhausted GPU
+// (qkrylov_debug_inject_alloc_failure).
+void device_alloc(void** p, size_t bytes);
+void device_free(void* p);
+int64_t live_device_allocs();
+void inject_alloc_failure(int64_t after_n);
 #define QKG_REQUIRE(cond, msg)                                                \
     do {                                                                      \
         if (!(cond)) throw ::qkg::Error(::qkg::INVALID_ARG, std::string(msg)); \

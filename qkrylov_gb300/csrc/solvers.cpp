@@ -418,6 +418,13 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
     auto& betas = out.betas;
     double e_old = 1e100;
     std::vector<cd> c;
+    // o.selective: instead of the reference's full reorthogonalisation, the
+    // mixed form's scheme in FP64 (Parlett-Scott: once the lowest Ritz pair's
+    // residual estimate |beta_k s_k| <= sqrt(eps_64) ||T||, later vectors are
+    // kept orthogonal to its Ritz vector) -- the control that separates the
+    // mixed form's precision from its reorthogonalisation
+    VecList<double2> psi(n);
+    const double so_tol = 1.5e-8;  // sqrt(eps_fp64)
     LaunchTimer timer(st);
     const auto t0 = clk::now();
     for (int iter = 0; iter < nmax; ++iter) {
@@ -431,24 +438,53 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
         out.t_spmv += timer.collect();
         ++out.n_spmv;
         alphas.push_back(alpha);
-        lanczos_update_f64(w.as<double2>(), v, vp, alpha, iter > 0 ? betas.back() : 0.0, n, ws, st);
-        // full reorthogonalisation against every stored vector (:148-151), one CGS pass
-        const int k = (int)V.size();
-        c.assign(k, 0.0);
-        mdot_f64(V.dev(), k, w.as<double2>(), n, c.data(), ws, st);
-        for (auto& x : c) x = -x;
-        mcombine_f64(V.dev(), k, c.data(), w.as<double2>(), n, ws, st);
-        const double beta = std::sqrt(nrm2sq_f64(w.as<double2>(), n, ws, st));
+        double b2 = lanczos_update_f64(w.as<double2>(), v, vp, alpha, iter > 0 ? betas.back() : 0.0, n, ws, st);
+        if (!o.selective) {
+            // full reorthogonalisation against every stored vector (:148-151), one CGS pass
+            const int k = (int)V.size();
+            c.assign(k, 0.0);
+            mdot_f64(V.dev(), k, w.as<double2>(), n, c.data(), ws, st);
+            for (auto& x : c) x = -x;
+            mcombine_f64(V.dev(), k, c.data(), w.as<double2>(), n, ws, st);
+            b2 = nrm2sq_f64(w.as<double2>(), n, ws, st);
+        } else if (psi.size()) {
+            c.assign(psi.size(), 0.0);
+            mdot_f64(psi.dev(), (int)psi.size(), w.as<double2>(), n, c.data(), ws, st);
+            for (auto& x : c) x = -x;
+            mcombine_f64(psi.dev(), (int)psi.size(), c.data(), w.as<double2>(), n, ws, st);
+            b2 = nrm2sq_f64(w.as<double2>(), n, ws, st);
+            ++out.n_selective;
+        }
+        const double beta = std::sqrt(b2);
         if (beta < 1e-15) { out.converged = true; break; }
         if (iter + 1 == nmax) break;
         betas.push_back(beta);
         double2* vn = V.push();
         QKG_CUDA(cudaMemcpyAsync(vn, w.p, n * sizeof(double2), cudaMemcpyDeviceToDevice, st));
         scal_f64(1.0 / beta, vn, n, st);
+        const int k = (int)alphas.size();
         if (iter > 0 && !o.fixed_steps) {
-            const double e = tridiag_lowest(alphas.data(), betas.data(), (int)alphas.size());
+            const double e = tridiag_lowest(alphas.data(), betas.data(), k);
             if (std::abs(e - e_old) < o.tol) { out.converged = true; break; }
             e_old = e;
+        }
+        if (o.selective && psi.size() == 0 && k >= 4) {
+            std::vector<double> d, z;
+            tridiag_eig(alphas.data(), betas.data(), k, d, {k - 1}, z);
+            int mi = 0;
+            for (int j = 1; j < k; ++j) if (d[j] < d[mi]) mi = j;
+            double tn = 0.0;
+            for (double x : d) tn = std::max(tn, std::abs(x));
+            if (beta * std::abs(z[mi]) <= so_tol * tn) {
+                std::vector<double> s;
+                tridiag_ground(alphas.data(), betas.data(), k, s);
+                std::vector<cd> cc(s.begin(), s.end());
+                double2* ps = psi.push();
+                QKG_CUDA(cudaMemsetAsync(ps, 0, n * sizeof(double2), st));
+                mcombine_f64(V.dev(), k, cc.data(), ps, n, ws, st);
+                const double pn = std::sqrt(nrm2sq_f64(ps, n, ws, st));
+                scal_f64(1.0 / pn, ps, n, st);
+            }
         }
     }
     QKG_CUDA(cudaStreamSynchronize(st));
@@ -802,6 +838,12 @@ DavidsonOut davidson_impl(Hamiltonian& H, int n_eig, int max_sub, double tol, bo
     n_eig = (int)std::min<uint64_t>((uint64_t)n_eig, n);
     max_sub = std::max(max_sub, 2 * n_eig);
     QKG_REQUIRE(max_sub + n_eig <= 1024, "Davidson: subspace limited to 1024 vectors");
+    // the Krylov space a mixed Lanczos left on the Hamiltonian is released
+    // first: the Davidson vectors come from their own pool
+    {
+        const auto ws_lock = H.workspace_lock();
+        H.release_workspace();
+    }
     Workspace ws(ws_cap(4 * (max_sub + n_eig + 2)));  // block projections: 4 right-hand vectors
     DBuf diag(n * sizeof(double2)), tmp, d64(n * sizeof(double2));
     H.diagonal_f64(diag.as<double2>(), st);

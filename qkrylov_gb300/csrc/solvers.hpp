@@ -71,6 +71,7 @@ struct LanczosOpts {
     uint64_t seed = 0;
     bool f32_stream = false;     // draw the start vector as the reference's FP32 engine does
     cd* evec_out = nullptr;      // with want_vec: the Ritz vector goes here (reference order) instead of LanczosOut::evec
+    bool selective = false;      // FP64 form: selective instead of full reorthogonalisation (the mixed form's scheme)
 };
 struct LanczosOut {
     double energy = 0.0;       // reported energy (refined for the mixed form)

@@ -5,12 +5,16 @@ profiles are taken with).
     python -m qkrylov_gb300.timing --L 22 --block 32 --steps 3 --vpl 4
     python -m qkrylov_gb300.timing --model hubbard --L 14 --davidson 4 --iters 14
 
+    python -m qkrylov_gb300.timing --peaks
+
 The second form runs the batched Lanczos on every Sz sector of the chain (or
 the Sz = 0 sector alone with ``--sz0-only``) with ``--block`` Philox start
 vectors per sector and reports the block-SpMV time.  The third runs the
 Davidson solver for the ``--davidson`` lowest states (subspace 32, mixed form
 unless ``--precision fp64``) for ``--iters`` iterations, twice, and reports
-the seconds per iteration of the second run.
+the seconds per iteration of the second run.  ``--peaks`` compiles and runs
+``peaks.cu`` (FP64/FP32 FMA rates, L2 and DRAM read bandwidth, scattered
+8-byte reads from shared memory and L1) and prints its JSON line.
 
 Builds the Hamiltonian (Heisenberg chain ``Sz Sz + 0.5 (S+ S- + S- S+)`` per
 bond, or Fermi-Hubbard chain ``-t c^dag c`` hopping per spin and direction plus
@@ -21,6 +25,8 @@ mean launch time and the algorithmic bandwidth (read x once, write y once).
 """
 import argparse
 import json
+import os
+import subprocess
 import time
 
 import qkrylov_gb300 as qk
@@ -54,7 +60,7 @@ def main():
     p.add_argument("--L", type=int, default=28)
     p.add_argument("--obc", action="store_true")
     p.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
-    p.add_argument("--mode", type=int, default=0, help="0 autotuned, 1 generic, 2 fast, 3 fast staged, 4 fast rows4, 5 rows4 staged")
+    p.add_argument("--mode", type=int, default=0, help="0 autotuned, 1 generic, 2 fast, 3 fast staged, 4 fast rows4, 5 rows4 staged, 6 rows4 wide, 7/8/9 tiled over 1/2/4 blocks")
     p.add_argument("--reps", type=int, default=5)
     p.add_argument("--block", type=int, default=0, help="vectors per sector: batched Lanczos over all Sz sectors")
     p.add_argument("--steps", type=int, default=3)
@@ -62,7 +68,10 @@ def main():
     p.add_argument("--sz0-only", action="store_true", help="block mode on the Sz = 0 sector alone")
     p.add_argument("--davidson", type=int, default=0, help="states for a Davidson run (0: SpMV timing)")
     p.add_argument("--iters", type=int, default=14, help="Davidson iterations")
+    p.add_argument("--peaks", action="store_true", help="FMA / L2 / DRAM / gather throughput probes")
     a = p.parse_args()
+    if a.peaks:
+        return peaks()
     if a.block:
         return block(a)
     if a.davidson:
@@ -77,9 +86,20 @@ def main():
     ms = H.benchmark_apply(fp32=fp32, reps=a.reps)
     n = H.dimension
     e = 8 if fp32 else 16
+    variant, tuned = H.tuning(fp32=fp32)
     print(json.dumps({"model": a.model, "L": a.L, "pbc": not a.obc, "dim": n, "precision": a.precision,
                       "mode": a.mode, "fast": fast, "ms": ms, "alg_GBs": 2 * n * e / ms / 1e6,
-                      "construct_s": round(tc, 3)}), flush=True)
+                      "construct_s": round(tc, 3), "autotuned": variant,
+                      "tuned_ms": {k: round(v, 4) for k, v in tuned.items() if v}}), flush=True)
+
+
+def peaks():
+    from qkrylov_gb300 import build as b
+    here = os.path.dirname(os.path.abspath(__file__))
+    exe = os.path.join(b.BUILD, "peaks")
+    os.makedirs(b.BUILD, exist_ok=True)
+    subprocess.run([b._nvcc()] + b.ARCH + ["-O3", "-o", exe, os.path.join(here, "peaks.cu")], check=True)
+    subprocess.run([exe], check=True)
 
 
 def block(a):

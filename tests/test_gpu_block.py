@@ -12,7 +12,17 @@ pytestmark = pytest.mark.gpu
 
 EARLY_RTOL = 1e-10   # FP64 alphas/betas of the first steps (before loss of orthogonality amplifies rounding)
 OBS_RTOL = 1e-8      # FP64 Z, E, Cv and S(omega)
-MIXED_RTOL = 1e-4    # FP32 vectors / FP64 reductions against FP64
+# FP32 Krylov vectors with FP64-accurate reductions against the FP64 form: the
+# bounds are about five times the largest errors measured on GB300 at these
+# sizes and at L = 10..18 (FTLM: relative dZ <= 6.1e-7, |dE| <= 7.3e-8,
+# |dCv| <= 2.0e-7; S(omega): relative <= 3.6e-6).  They sit at the FP32
+# storage rounding of the vectors (2^-24 = 6e-8) times each observable's
+# conditioning, which no reduction accuracy removes; the FP64 forms are held
+# to OBS_RTOL.
+MIXED_Z_RTOL = 3e-6
+MIXED_E_ATOL = 4e-7
+MIXED_CV_ATOL = 1e-6
+MIXED_S_RTOL = 2e-5
 
 
 def chain_sectors(qk, L, pbc=True):
@@ -111,9 +121,9 @@ def test_ftlm_sectors_mixed_vs_fp64(qk):
     r32 = qk.ftlm_sectors(hams, betas, n_random=R, n_steps=Mst, mixed=True, start="ftlm", shifted=True)
     z64 = r64.partition_function * np.exp(r64.log_shift - r64.log_shift)
     z32 = r32.partition_function * np.exp(r32.log_shift - r64.log_shift)
-    np.testing.assert_allclose(z32, z64, rtol=MIXED_RTOL)
-    np.testing.assert_allclose(r32.internal_energy, r64.internal_energy, rtol=MIXED_RTOL, atol=MIXED_RTOL)
-    np.testing.assert_allclose(r32.specific_heat, r64.specific_heat, rtol=MIXED_RTOL, atol=MIXED_RTOL)
+    np.testing.assert_allclose(z32, z64, rtol=MIXED_Z_RTOL)
+    np.testing.assert_allclose(r32.internal_energy, r64.internal_energy, rtol=0, atol=MIXED_E_ATOL)
+    np.testing.assert_allclose(r32.specific_heat, r64.specific_heat, rtol=0, atol=MIXED_CV_ATOL)
 
 
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
@@ -144,7 +154,7 @@ def test_cf_block_matches_oracle(qk, oracle, mixed):
             assert np.abs(res[i].alphas[:k] - a[:k]).max() <= EARLY_RTOL * max(1.0, np.abs(a).max())
         S = np.array([qk.evaluate_spectral_function(res[i], w, -3.0, eta=0.2) for w in omegas])
         So = np.array([spectral(oracle, a, bb, nrm, w, -3.0, 0.2) for w in omegas])
-        tol = OBS_RTOL if not mixed else MIXED_RTOL
+        tol = OBS_RTOL if not mixed else MIXED_S_RTOL
         assert np.abs(S - So).max() <= tol * np.abs(So).max()
 
 
@@ -206,7 +216,7 @@ def test_structure_factor_block(qk, oracle, mixed):
     for k in range(1, len(phis)):
         a, bb, nrm = oh.cf(phis[k], 60)
         So = np.array([spectral(oracle, a, bb, nrm, w, E0, 0.05) for w in omegas])
-        tol = OBS_RTOL if not mixed else MIXED_RTOL
+        tol = OBS_RTOL if not mixed else MIXED_S_RTOL
         assert np.abs(S[k] - So).max() <= tol * np.abs(So).max()
 
 

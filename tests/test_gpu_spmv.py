@@ -83,8 +83,9 @@ def test_entries_bit_exact(qk, name):
     np.testing.assert_allclose(vals, g["csr_vals"], rtol=0, atol=1e-15)
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6],
-                         ids=["auto", "generic", "fast", "fast-staged", "fast-rows4", "fast-rows4-staged", "fast-rows4-wide"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10],
+                         ids=["auto", "generic", "fast", "fast-staged", "fast-rows4", "fast-rows4-staged", "fast-rows4-wide",
+                              "tile1", "tile2", "tile4", "class"])
 @pytest.mark.parametrize("name", golden_names())
 def test_apply_and_diagonal(qk, name, mode):
     g = load_golden(name)
@@ -126,14 +127,15 @@ def test_apply_against_oracle(qk, oracle, model, N, sector, terms):
     rng = np.random.default_rng(7)
     x = rng.normal(size=o.dim) + 1j * rng.normal(size=o.dim)
     yo = o.apply(x)
-    for mode in (0, 1, 2, 3, 4, 5, 6):
+    waits0 = qk.device_wait_timeouts()
+    for mode in (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10):
         H.select_kernel(mode=mode)
         y = H.apply(x)
         assert np.abs(y - yo).max() <= RTOL64 * np.abs(yo).max()
         y32 = apply32(qk, H, x)
         assert np.abs(y32 - yo).max() <= RTOL32 * 10 * np.abs(yo).max()
     # the staged kernels' bounded waits for their asynchronous copies never gave up
-    assert qk.device_wait_timeouts() == 0
+    assert qk.device_wait_timeouts() == waits0
 
 
 def test_edge_cases(qk):
@@ -260,9 +262,17 @@ def test_full_size_heisenberg_L28_properties(qk, oracle):
     rng = np.random.default_rng(3)
     x = (rng.standard_normal(n) + 1j * rng.standard_normal(n))
     z = (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    waits0 = qk.device_wait_timeouts()
     hx, hz = H.apply(x), H.apply(z)
     lhs, rhs = np.vdot(z, hx), np.vdot(hz, x)
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    # every fast variant (the tiled ones included) gives the same y at full size
+    for mode in (4, 7, 8, 9, 10):
+        H.select_kernel(mode=mode)
+        assert np.abs(H.apply(x) - hx).max() <= RTOL64 * np.abs(hx).max(), mode
+        assert np.abs(apply32(qk, H, x) - hx).max() <= RTOL32 * 10 * np.abs(hx).max(), mode
+    H.select_kernel(mode=0)
+    assert qk.device_wait_timeouts() == waits0
     # exact rows from the oracle for three row windows (first, middle, last block)
     from oracle_ctypes import Oracle
     import ctypes as c

@@ -61,6 +61,33 @@ def test_noalloc_dot_matches_allocating_dot_on_consecutive_calls(qk):
         assert abs(v_new - np.vdot(x, y)) <= RTOL64 * scale
 
 
+def test_noalloc_dot_fills_every_scratch_slot_on_a_stream(qk):
+    """n = 8192 * 16384: all 16384 partial slots are written, the last one next
+    to the result slot; on a stream the caller created."""
+    L = qk.lib()
+    cudart = _cudart()
+    n = MAX_ELEMENTS
+    i = np.arange(n, dtype=np.int64)
+    y = ((i % 7) - 3).astype(np.float64) + 1j * ((i % 5) - 2).astype(np.float64)
+    x = np.ones(n, dtype=np.complex128)
+    exact = complex(float(((i % 7) - 3).sum()), float(((i % 5) - 2).sum()))  # sum of conj(1) * y
+    del i
+    dx, dy = _to_device(cudart, x), _to_device(cudart, y)
+    del x, y
+    st = ctypes.c_void_p()
+    assert cudart.cudaStreamCreate(ctypes.byref(st)) == 0
+    try:
+        out = np.zeros(2)
+        for _ in range(2):
+            assert L.qkrylov_vector_dot_device_f64_noalloc(dx, dy, n, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                           st) == 0
+            assert complex(out[0], out[1]) == exact  # small integers: every partial sum is exact
+    finally:
+        cudart.cudaStreamDestroy(st)
+        cudart.cudaFree(dx)
+        cudart.cudaFree(dy)
+
+
 def test_noalloc_dot_rejects_sizes_beyond_its_scratch(qk):
     L = qk.lib()
     out = np.zeros(2)
@@ -69,4 +96,5 @@ def test_noalloc_dot_rejects_sizes_beyond_its_scratch(qk):
     rc = L.qkrylov_vector_dot_device_f64_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16), MAX_ELEMENTS + 1, dp, None)
     assert rc == qk.ERROR_INVALID_ARG
     assert b"exceeds" in L.qkrylov_last_error()
+    # n = 0 is the warm-up call: it looks up the scratch array and loads the kernels, and computes nothing
     assert L.qkrylov_vector_dot_device_f64_noalloc(None, None, 0, dp, None) == 0 and out[0] == 0.0
