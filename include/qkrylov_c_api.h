@@ -241,6 +241,22 @@ uint64_t qkrylov_kernel_launches(void);
  * which the count grew returns QKRYLOV_ERROR_DEVICE_TIMEOUT. */
 int qkrylov_device_wait_timeouts(uint32_t* count);
 
+/* Projections of device vectors (no counterpart in the reference; its
+ * Davidson forms them as separate dots, src/solvers/davidson.cpp:143-150,
+ * 213-223): out[2 (o k + j)], out[2 (o k + j) + 1] = Re, Im <V_j, W_o> for
+ * j < k, o < nw <= 4, where V_j = v_dev[j] and W_o = w_dev[o] are host arrays
+ * of device pointers to n complex FP32 elements (16-byte aligned).
+ * method 0: compensated CUDA-core kernel (FP64-accurate sums, k nw <= 4088);
+ * method 1: tensor cores (tcgen05, each product as hi*hi + hi*lo + lo*hi of
+ * TF32 splits, FP32 sums of about a thousand products added in FP64;
+ * k <= 128).  Waits for `stream`. */
+int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
+                                   int method, double* out, void* stream);
+/* Kernel the solvers' FP32 projections use (the mixed Davidson's projected
+ * matrix and Gram-Schmidt passes): 0 the compensated CUDA-core kernel (the
+ * default), 1 the tensor-core kernel where it applies.  Process-wide. */
+int qkrylov_set_projection_kernel(int method);
+
 /* Test hooks (no counterpart in the reference).
  * qkrylov_debug_inject_alloc_failure: the after_n-th device allocation of the
  * library from now on (0: the next one) fails as cudaMalloc does on an

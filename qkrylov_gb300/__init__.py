@@ -115,6 +115,9 @@ _SIGS = {
     "qkrylov_kernel_launches": (_u64, []),
     "qkrylov_device_wait_timeouts": (_i, [_c.POINTER(_c.c_uint32)]),
     "qkrylov_debug_inject_alloc_failure": (_i, [_c.c_int64]),
+    "qkrylov_vector_mdot_device_f32": (_i, [_c.POINTER(_c.c_void_p), _i, _c.POINTER(_c.c_void_p), _i, _c.c_uint64, _i,
+                                            _dp, _vp]),
+    "qkrylov_set_projection_kernel": (_i, [_i]),
     "qkrylov_debug_live_allocations": (_c.c_int64, []),
     "qkrylov_debug_device_wait_probe": (_i, [_c.c_int64]),
     "qkrylov_vector_dot_device_f64": (_i, [_vp, _vp, _u64, _dp, _vp]),
@@ -516,6 +519,12 @@ def device_wait_timeouts():
     if rc not in (0, -4):
         _check(rc)
     return int(c.value)
+
+
+def set_projection_kernel(method):
+    """Kernel of the solvers' FP32 projections: "cuda" (compensated CUDA-core,
+    FP64-accurate; the default) or "tensor" (tcgen05 tensor cores, 3xTF32)."""
+    _check(lib().qkrylov_set_projection_kernel({"cuda": 0, "tensor": 1}[method]))
 
 
 def set_device(device_id):

@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libqkrylov_gb300.so")
-SOURCES = ["hamiltonian.cu", "spmv_tile.cu", "krylov.cu", "lanczos_dev.cu", "noalloc.cu", "block.cu", "basis.cpp", "compile.cpp", "solvers.cpp",
+SOURCES = ["hamiltonian.cu", "spmv_tile.cu", "krylov.cu", "lanczos_dev.cu", "noalloc.cu", "mdot_tc.cu", "block.cu", "basis.cpp", "compile.cpp", "solvers.cpp",
            "c_api.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -582,6 +582,36 @@ int qkrylov_device_wait_timeouts(uint32_t* count) {
     if (*count) rc = QKRYLOV_ERROR_DEVICE_TIMEOUT;
     return rc;
 }
+int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
+                                   int method, double* out, void* stream) {
+    if (!v_dev || !w_dev || !out || k < 1 || nw < 1 || nw > 4 || (method != 0 && method != 1))
+        return QKRYLOV_ERROR_INVALID_ARG;
+    if (method == 1 && !qkg::mdot_tc_supported(k, nw)) return QKRYLOV_ERROR_INVALID_ARG;
+    if (method == 0 && (size_t)k * nw > 4088) return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        qkg::DBuf tab((size_t)k * sizeof(void*));
+        QKG_CUDA(cudaMemcpyAsync(tab.p, v_dev, (size_t)k * sizeof(void*), cudaMemcpyHostToDevice, s));
+        std::vector<float2*> w(nw);
+        for (int o = 0; o < nw; ++o) w[o] = const_cast<float2*>(static_cast<const float2*>(w_dev[o]));
+        qkg::Workspace ws(1 << 16);
+        std::vector<cd> r((size_t)k * nw);
+        const auto* V = static_cast<const float2* const*>(tab.p);
+        if (method == 1) qkg::mdot_multi_f32_tc(V, k, w.data(), nw, n, r.data(), ws, s);
+        else qkg::mdot_multi_f32_cuda(V, k, w.data(), nw, n, r.data(), ws, s);
+        for (size_t i = 0; i < r.size(); ++i) {
+            out[2 * i] = r[i].real();
+            out[2 * i + 1] = r[i].imag();
+        }
+    });
+}
+
+int qkrylov_set_projection_kernel(int method) {
+    if (method != 0 && method != 1) return QKRYLOV_ERROR_INVALID_ARG;
+    qkg::set_projection_mode(method);
+    return QKRYLOV_SUCCESS;
+}
+
 int qkrylov_debug_inject_alloc_failure(int64_t after_n) {
     qkg::inject_alloc_failure(after_n);
     return QKRYLOV_SUCCESS;

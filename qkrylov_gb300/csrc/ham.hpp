@@ -231,6 +231,8 @@ private:
     FastSet f64s_, f32s_;
     DBuf iptr_, ient_;
     DBuf optr_, mptr_, ment_;  // per-block outer-entry / straddling-term list offsets and straddling entries
+    DBuf srank_;               // straddling terms' target inner ranks per inner configuration
+    uint32_t srank_stride_ = 0;
 
     std::shared_ptr<Basis> basis_;
     const DevBasis* db_ = nullptr;
@@ -287,6 +289,19 @@ void mdot_f32(const float2* const* V_dev, int k, const float2* w, uint64_t n, st
 // all W_o (compensated FP32; W a host array of device pointers).
 void mdot_multi_f32(const float2* const* V_dev, int k, float2* const* W, int nw, uint64_t n,
                     std::complex<double>* out, Workspace& ws, cudaStream_t s);
+// The compensated CUDA-core kernel whatever the projection mode.
+void mdot_multi_f32_cuda(const float2* const* V_dev, int k, float2* const* W, int nw, uint64_t n,
+                         std::complex<double>* out, Workspace& ws, cudaStream_t s);
+// The same on the tensor cores (tcgen05, 3xTF32 products, FP32 accumulation
+// read out into FP64 every thousand or so terms; mdot_tc.cu): k <= 128, nw <= 4.
+bool mdot_tc_supported(int k, int nw);
+size_t mdot_tc_smem(int k, int nw);
+void mdot_multi_f32_tc(const float2* const* V_dev, int k, float2* const* W, int nw, uint64_t n,
+                       std::complex<double>* out, Workspace& ws, cudaStream_t s);
+// Which kernel mdot_multi_f32 uses: 0 the compensated CUDA-core kernel
+// (FP64-accurate), 1 the tensor-core kernel where it applies.
+void set_projection_mode(int mode);
+int projection_mode();
 // w += sum_j c[j] V_j  (c given on the host, k <= 1024)
 void mcombine_f64(const double2* const* V_dev, int k, const std::complex<double>* c, double2* w, uint64_t n,
                   Workspace& ws, cudaStream_t s);

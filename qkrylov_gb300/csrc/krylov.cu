@@ -18,6 +18,7 @@
 #include "fast_common.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace qkg {
 
@@ -631,8 +632,24 @@ void mdot_f32(const float2* const* V, int k, const float2* w, uint64_t n, std::c
               cudaStream_t s) {
     mdot_impl<float2, true>(V, k, w, n, out, ws, s);
 }
+namespace {
+std::atomic<int> g_projection_mode{0};
+}
+void set_projection_mode(int mode) { g_projection_mode.store(mode); }
+int projection_mode() { return g_projection_mode.load(); }
+
 void mdot_multi_f32(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,
                     Workspace& ws, cudaStream_t s) {
+    if (k <= 0 || nw <= 0) return;
+    if (g_projection_mode.load() == 1 && mdot_tc_supported(k, nw)) {
+        mdot_multi_f32_tc(V, k, W, nw, n, out, ws, s);
+        return;
+    }
+    mdot_multi_f32_cuda(V, k, W, nw, n, out, ws, s);
+}
+
+void mdot_multi_f32_cuda(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,
+                         Workspace& ws, cudaStream_t s) {
     if (k <= 0 || nw <= 0) return;
     QKG_REQUIRE(nw <= 4 && (size_t)k * nw <= 4088, "mdot_multi: at most 4 right-hand vectors and 4088 products");
     // the W pointer table goes through the result slots (read by the kernel before finish overwrites them)
