@@ -98,12 +98,6 @@ struct FastParams {
     const OutEnt<A>* oent;
     const uint32_t* mptr;
     const uint2* ment;
-    // Straddling terms' inner parts, tabulated: srank[t * srank_stride + i] is
-    // the target inner rank of straddling term t on the inner configuration
-    // inner_state[i] (kEllEmpty where the term's inner conditions fail); null
-    // when not built (the kernels then rank per row through inner_rank).
-    const uint32_t* srank;
-    uint32_t srank_stride;
     int diag_mode;
     int n_dtab;
     const void* dcode;

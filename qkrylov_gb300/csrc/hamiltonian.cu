@@ -682,43 +682,27 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         const KTerm<uint32_t, A> t = p.mixed[mk.x];
         uint32_t idx[RT];
         bool ok[RT];
-        if (p.srank) {
-            // the inner part from the table (the block's list already holds the
-            // outer part): one coalesced read per row
-            const uint32_t* __restrict__ sr = p.srank + (size_t)mk.x * p.srank_stride + it.inner_base + pass + tbase;
 #pragma unroll
-            for (int q = 0; q < RT; ++q) {
-                const uint32_t r2 = live[q] ? __ldg(sr + 32 * q) : kEllEmpty;
-                ok[q] = r2 != kEllEmpty;
-                if (ok[q] && (t.flags & 1u))
-                    ok[q] = in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N,
-                                          s[q] ^ t.X);
-                idx[q] = mk.y + (ok[q] ? r2 : 0u);
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < RT; ++q) {
-                ok[q] = live[q] && (s[q] & t.C) == t.V;
-                const uint32_t s2 = s[q] ^ t.X;
-                if (ok[q] && (t.flags & 1u))
-                    ok[q] = in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2);
-                idx[q] = 0;
-                if (ok[q]) {
-                    const uint32_t b2 = s2 & p.in_mask;
-                    idx[q] = mk.y + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
-                }
+        for (int q = 0; q < RT; ++q) {
+            ok[q] = live[q] && (s[q] & t.C) == t.V;
+            const uint32_t s2 = s[q] ^ t.X;
+            if (ok[q] && (t.flags & 1u))
+                ok[q] = in_basis_fast(p.ngroups, p.gmask0, p.gmask1, p.gpop0, p.gpop1, p.no_double, p.N, s2);
+            idx[q] = 0;
+            if (ok[q]) {
+                const uint32_t b2 = s2 & p.in_mask;
+                idx[q] = mk.y + (p.inner_rank ? __ldg(p.inner_rank + b2) : b2);
             }
         }
         T2 xv[RT];
 #pragma unroll
         for (int q = 0; q < RT; ++q)
             if (ok[q]) xv[q] = x[idx[q]];
-        const bool plain_amp = ((t.flags >> 8) & 0xffu) == 0 && t.J == 0;  // no variable factors, no signs
 #pragma unroll
         for (int q = 0; q < RT; ++q) {
             if (!ok[q]) continue;
-            A cr = t.ar, ci = t.ai;
-            if (!plain_amp) term_amp<uint32_t, A>(t, s[q], p.vars, cr, ci);
+            A cr, ci;
+            term_amp<uint32_t, A>(t, s[q], p.vars, cr, ci);
             cmac<A>(ar_[q], ai_[q], cr, ci, xv[q], REAL);
         }
     }
@@ -1114,28 +1098,6 @@ void Hamiltonian::build_fast() {
     upload_vec(optr_, optr);
     upload_vec(mptr_, mptr);
     upload_vec(ment_, ment);
-    // Straddling terms' inner parts per inner configuration (inner_state
-    // order): the rank of the flipped inner configuration in its class, or
-    // kEllEmpty where the term's inner conditions fail.  The four-row kernels
-    // then read it coalesced instead of ranking scattered configurations.
-    srank_.reset();
-    srank_stride_ = 0;
-    if (!mixed.empty() && mixed.size() <= 64 && B.n_in <= 16) {
-        const uint32_t P = 1u << B.n_in;
-        std::vector<uint32_t> sr((size_t)mixed.size() * P, kEllEmpty);
-        for (size_t t = 0; t < mixed.size(); ++t) {
-            const HostTerm& h = *mixed[t];
-            const uint32_t ci = (uint32_t)(h.C & inm), vi = (uint32_t)(h.V & inm), xi = (uint32_t)(h.X & inm);
-            for (uint32_t i = 0; i < P; ++i) {
-                const uint32_t b = B.inner_all ? i : B.inner_state[i];
-                if ((b & ci) != vi) continue;
-                const uint32_t b2 = b ^ xi;
-                sr[(size_t)t * P + i] = B.inner_all ? b2 : B.inner_rank[b2];
-            }
-        }
-        upload_vec(srank_, sr);
-        srank_stride_ = P;
-    }
     auto build = [&](auto tag, FastSet& fs) {
         using A = decltype(tag);
         std::vector<KTerm<uint32_t, A>> ko, ki, km;
@@ -1420,8 +1382,6 @@ void Hamiltonian::fast_params(FastParams<A>& p) const {
     p.oent = fs.oent.as<OutEnt<A>>();
     p.mptr = mptr_.as<uint32_t>();
     p.ment = ment_.as<uint2>();
-    p.srank = srank_.as<uint32_t>();
-    p.srank_stride = srank_stride_;
     p.diag_mode = diag_mode_;
     const DBuf& dtab = sizeof(A) == 8 ? dtab64_ : dtab32_;
     p.n_dtab = (int)(dtab.bytes / (2 * sizeof(A)));
@@ -1433,7 +1393,7 @@ uint32_t spmv_wait_timeouts() {
     QKG_CUDA(cudaDeviceSynchronize());
     uint32_t c = 0;
     QKG_CUDA(cudaMemcpyFromSymbol(&c, g_spmv_wait_timeouts, sizeof(c)));
-    return c + tilek::tile_wait_timeouts();
+    return c + tilek::tile_wait_timeouts() + tc_wait_timeouts();
 }
 
 uint32_t Hamiltonian::tile_slot_elems(size_t elem_bytes) const { return tilek::tile_slot(max_block_, elem_bytes); }
