@@ -47,6 +47,8 @@ inline int tile_index(int g) { return g == 1 ? 0 : g == 2 ? 1 : 2; }
 // Bounded device waits of the SpMV kernels that gave up on the current GPU
 // (waits for the GPU first).
 uint32_t spmv_wait_timeouts();
+// bounded waits of the tensor-core projection kernel that gave up (part of the above)
+uint32_t tc_wait_timeouts();
 namespace tilek {
 // Test hook: one bounded wait (limit_ns of global time, clamped to 1 us .. 1 s)
 // on an mbarrier that nothing completes, counted as a give-up.
@@ -231,8 +233,6 @@ private:
     FastSet f64s_, f32s_;
     DBuf iptr_, ient_;
     DBuf optr_, mptr_, ment_;  // per-block outer-entry / straddling-term list offsets and straddling entries
-    DBuf srank_;               // straddling terms' target inner ranks per inner configuration
-    uint32_t srank_stride_ = 0;
 
     std::shared_ptr<Basis> basis_;
     const DevBasis* db_ = nullptr;

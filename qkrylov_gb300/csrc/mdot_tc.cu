@@ -36,6 +36,8 @@
 
 #include <algorithm>
 #include <mutex>
+#include <map>
+#include <array>
 
 namespace qkg {
 
@@ -126,11 +128,13 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, ui
         : "memory");
 }
 
-template <int NW>
+// LPT: B chunks one thread loads per stage (16 k / 256 rounded up: 2, 4 or 8).
+template <int NW, int LPT>
 __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const* __restrict__ V, int k,
                                                              const float2* const* __restrict__ W, uint64_t n,
                                                              uint64_t stages_per_cta, uint32_t np, uint32_t tcols,
-                                                             double2* __restrict__ part, int stride) {
+                                                             double2* __restrict__ part, int stride,
+                                                             unsigned int* __restrict__ fail) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     // 1 KB alignment for the swizzle atoms
     unsigned char* base = reinterpret_cast<unsigned char*>(
@@ -177,28 +181,55 @@ __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const
     uint32_t chunk_fill = 0;
     uint32_t commits[2] = {0u, 0u};  // thread 0: MMA commits per stage
 
+    const uint32_t nbj = (uint32_t)k * 8u * kTcKc;  // 16-byte chunks of B per stage
+    const bool has_a = tid < (uint32_t)NW * 8u * kTcKc;
+    // This thread's loads of one stage (B: rows j < k, chunk c of K chunk q; A:
+    // the right-hand vectors).  The next stage's loads are issued before this
+    // stage waits and synchronises, so a DRAM round trip overlaps each stage.
+    float4 vb[LPT], wa = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto load_stage = [&](uint64_t st, float4* out_b, float4& out_a) {
+        const uint64_t f0 = st * 16ull * kTcKc;
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) {
+            const uint32_t i = tid + (uint32_t)u * kTcThreads;
+            if (i < nbj) {
+                const uint32_t j = i / (8u * kTcKc), rem = i % (8u * kTcKc);
+                out_b[u] = load2(V[j], f0 + 16ull * (rem >> 3) + 2ull * (rem & 7u), n);
+            }
+        }
+        if (has_a) {
+            const uint32_t o = tid / (8u * kTcKc), rem = tid % (8u * kTcKc);
+            out_a = load2(W[o], f0 + 16ull * (rem >> 3) + 2ull * (rem & 7u), n);
+        }
+    };
+    if (s_begin < s_end) load_stage(s_begin, vb, wa);
     for (uint64_t s = s_begin; s < s_end && ok; ++s) {
         const uint32_t it = (uint32_t)(s - s_begin), b = it & 1u;
         unsigned char* sb = stage[b];
+        float4 nb[LPT], na = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (s + 1 < s_end) load_stage(s + 1, nb, na);
         // the MMAs that read this stage two iterations ago are complete
         if (it >= 2 && !tc_wait(bar[b], ((it - 2) >> 1) & 1u)) {
-            if (lane == 0) atomicAdd(&g_tc_errors, 1u);
+            if (lane == 0) {
+                atomicAdd(&g_tc_errors, 1u);
+                atomicAdd(fail, 1u);
+            }
             s_fail = 1;
         }
-        const uint64_t e0 = s * 16ull * kTcKc;  // first complex element of the stage
-        // B: rows j < k, 16-byte chunks c of the stage's kTcKc K chunks
-        const uint32_t nbj = (uint32_t)k * 8u * kTcKc;
-        for (uint32_t i = tid; i < nbj; i += kTcThreads) {
-            const uint32_t j = i / (8u * kTcKc), rem = i % (8u * kTcKc), q = rem >> 3, c = rem & 7u;
-            const float4 v = load2(V[j], e0 + 16ull * q + 2ull * c, n);
-            const float4 h = hi4(v);
-            *reinterpret_cast<float4*>(sb + sm.b_hi(q) + sw_off(j, c)) = h;
-            *reinterpret_cast<float4*>(sb + sm.b_lo(q) + sw_off(j, c)) = lo4(v, h);
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) {
+            const uint32_t i = tid + (uint32_t)u * kTcThreads;
+            if (i < nbj) {
+                const uint32_t j = i / (8u * kTcKc), rem = i % (8u * kTcKc), q = rem >> 3, c = rem & 7u;
+                const float4 h = hi4(vb[u]);
+                *reinterpret_cast<float4*>(sb + sm.b_hi(q) + sw_off(j, c)) = h;
+                *reinterpret_cast<float4*>(sb + sm.b_lo(q) + sw_off(j, c)) = lo4(vb[u], h);
+            }
         }
         // A: rows 2o (W_o) and 2o + 1 (W_o rotated)
-        for (uint32_t i = tid; i < (uint32_t)NW * 8u * kTcKc; i += kTcThreads) {
-            const uint32_t o = i / (8u * kTcKc), rem = i % (8u * kTcKc), q = rem >> 3, c = rem & 7u;
-            const float4 w = load2(W[o], e0 + 16ull * q + 2ull * c, n);
+        if (has_a) {
+            const uint32_t o = tid / (8u * kTcKc), rem = tid % (8u * kTcKc), q = rem >> 3, c = rem & 7u;
+            const float4 w = wa;
             const float4 wr = make_float4(w.y, -w.x, w.w, -w.z);
             const float4 h = hi4(w), hr = hi4(wr);
             *reinterpret_cast<float4*>(sb + sm.a_hi(q) + sw_off(2 * o, c)) = h;
@@ -206,6 +237,9 @@ __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const
             *reinterpret_cast<float4*>(sb + sm.a_hi(q) + sw_off(2 * o + 1, c)) = hr;
             *reinterpret_cast<float4*>(sb + sm.a_lo(q) + sw_off(2 * o + 1, c)) = lo4(wr, hr);
         }
+#pragma unroll
+        for (int u = 0; u < LPT; ++u) vb[u] = nb[u];
+        wa = na;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -235,7 +269,10 @@ __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const
         // read the accumulator out every kTcChunkStages stages and at the end
         if (chunk_fill == (uint32_t)kTcChunkStages || s + 1 == s_end) {
             if (!tc_wait(bar[b], (it >> 1) & 1u)) {
-                if (lane == 0) atomicAdd(&g_tc_errors, 1u);
+                if (lane == 0) {
+                atomicAdd(&g_tc_errors, 1u);
+                atomicAdd(fail, 1u);
+            }
                 s_fail = 1;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -308,13 +345,47 @@ __global__ void tc_finish_kernel(const double2* __restrict__ part, int nparts, i
     }
 }
 
-uint32_t tc_errors() {
+template <int LPT>
+void allow_tc(int lim) {
+    QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<1, LPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<2, LPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<3, LPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<4, LPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+}
+template <int LPT>
+void launch_tc(int nw, int g, size_t smem, cudaStream_t s, const float2* const* V, int k, float2* const* dw, uint64_t n,
+               uint64_t per, uint32_t np, uint32_t tcols, double2* part, unsigned int* fail) {
+    switch (nw) {
+        case 1: mdot_tc_kernel<1, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
+        case 2: mdot_tc_kernel<2, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
+        case 3: mdot_tc_kernel<3, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
+        default: mdot_tc_kernel<4, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
+    }
+}
+
+// CTAs of the kernel for (nw, lpt) resident on the whole GPU at this shared memory
+// (the caller caches it).
+int tc_resident(int dev, int nw, int lpt, size_t smem) {
+    int sms = 0, per = 0;
+    QKG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const void* f = nullptr;
+    auto pick = [&](auto k1, auto k2, auto k3, auto k4) {
+        f = nw == 1 ? (const void*)k1 : nw == 2 ? (const void*)k2 : nw == 3 ? (const void*)k3 : (const void*)k4;
+    };
+    if (lpt == 2) pick(mdot_tc_kernel<1, 2>, mdot_tc_kernel<2, 2>, mdot_tc_kernel<3, 2>, mdot_tc_kernel<4, 2>);
+    else if (lpt == 4) pick(mdot_tc_kernel<1, 4>, mdot_tc_kernel<2, 4>, mdot_tc_kernel<3, 4>, mdot_tc_kernel<4, 4>);
+    else pick(mdot_tc_kernel<1, 8>, mdot_tc_kernel<2, 8>, mdot_tc_kernel<3, 8>, mdot_tc_kernel<4, 8>);
+    QKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kTcThreads, smem));
+    return std::max(1, per) * std::max(1, sms);
+}
+
+}  // namespace
+
+uint32_t tc_wait_timeouts() {
     uint32_t c = 0;
     QKG_CUDA(cudaMemcpyFromSymbol(&c, g_tc_errors, sizeof(c)));
     return c;
 }
-
-}  // namespace
 
 size_t mdot_tc_smem(int k, int nw) {
     const uint32_t np = (uint32_t)(((k + 15) / 16) * 16);
@@ -334,44 +405,57 @@ void mdot_multi_f32_tc(const float2* const* V, int k, float2* const* W, int nw, 
     uint32_t tcols = 32;
     while (tcols < np) tcols <<= 1;
     const size_t smem = mdot_tc_smem(k, nw);
+    const int lpt = k <= 32 ? 2 : k <= 64 ? 4 : 8;
+    int dev = 0;
+    QKG_CUDA(cudaGetDevice(&dev));
+    int resident = 0;
     {
+        // per device: the shared-memory opt-in once, and the resident CTAs per
+        // (nw, k rounded up to 16)
         static std::mutex mu;
-        static uint64_t done = 0;
-        int dev = 0;
-        QKG_CUDA(cudaGetDevice(&dev));
+        static std::map<int, std::array<int, 33>> cache;  // [0]: opt-in done; [1 + 8 (nw-1) + np/16 - 1]
         std::lock_guard<std::mutex> lk(mu);
-        const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
-        if (!(bit && (done & bit))) {
+        auto& c = cache[dev];
+        if (!c[0]) {
             const int lim = (int)kTcSmemLimit;
-            QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-            QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-            QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-            QKG_CUDA(cudaFuncSetAttribute(mdot_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-            done |= bit;
+            allow_tc<2>(lim);
+            allow_tc<4>(lim);
+            allow_tc<8>(lim);
+            c[0] = 1;
         }
+        int& r = c[1 + 8 * (nw - 1) + (int)(np / 16) - 1];
+        if (!r) r = tc_resident(dev, nw, lpt, smem);
+        resident = r;
     }
-    // the W pointer table goes through the result slots (read by the kernel before the finish overwrites them)
-    float2** dw = reinterpret_cast<float2**>(ws.result.as<double2>() + 4096 - 8);
-    QKG_CUDA(cudaMemcpyAsync(dw, W, (size_t)nw * sizeof(float2*), cudaMemcpyHostToDevice, s));
+    // Host-side scratch in the pinned result slots: the W pointer table (copied in
+    // without staging) and the failure count of this call.
+    double2* hslot = reinterpret_cast<double2*>(ws.host);
+    double2* dslot = ws.result.as<double2>();
+    float2** hw = reinterpret_cast<float2**>(hslot + 4096 - 8);
+    for (int o = 0; o < nw; ++o) hw[o] = W[o];
+    float2** dw = reinterpret_cast<float2**>(dslot + 4096 - 8);
+    unsigned int* dfail = reinterpret_cast<unsigned int*>(dslot + 4096 - 16);
+    unsigned int* hfail = reinterpret_cast<unsigned int*>(hslot + 4096 - 16);
+    QKG_CUDA(cudaMemcpyAsync(dw, hw, (size_t)nw * sizeof(float2*), cudaMemcpyHostToDevice, s));
+    QKG_CUDA(cudaMemsetAsync(dfail, 0, sizeof(unsigned int), s));
     const uint64_t total = (n + 16ull * kTcKc - 1) / (16ull * kTcKc);
-    const uint64_t want = std::max<uint64_t>(1, std::min<uint64_t>(152ull * 4, ws.cap_partials / ((size_t)k * nw)));
+    // one wave: as many CTAs as can be resident at once
+    const uint64_t want =
+        std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)resident, ws.cap_partials / ((size_t)k * nw)));
     const uint64_t per = std::max<uint64_t>(1, (total + want - 1) / want);
     const int g = (int)std::max<uint64_t>(1, (total + per - 1) / per);
     QKG_REQUIRE((size_t)g * k * nw <= ws.cap_partials, "tensor-core projections: workspace too small");
-    const uint32_t before = tc_errors();
     double2* part = ws.partial.as<double2>();
-    switch (nw) {
-        case 1: mdot_tc_kernel<1><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g); break;
-        case 2: mdot_tc_kernel<2><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g); break;
-        case 3: mdot_tc_kernel<3><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g); break;
-        default: mdot_tc_kernel<4><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g); break;
-    }
+    if (lpt == 2) launch_tc<2>(nw, g, smem, s, V, k, dw, n, per, np, tcols, part, dfail);
+    else if (lpt == 4) launch_tc<4>(nw, g, smem, s, V, k, dw, n, per, np, tcols, part, dfail);
+    else launch_tc<8>(nw, g, smem, s, V, k, dw, n, per, np, tcols, part, dfail);
     QKG_LAUNCHED();
     tc_finish_kernel<<<k * nw, 256, 0, s>>>(part, g, g, ws.result.as<double2>());
     QKG_LAUNCHED();
     QKG_CUDA(cudaMemcpyAsync(ws.host, ws.result.p, (size_t)k * nw * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    QKG_CUDA(cudaMemcpyAsync(hfail, dfail, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     QKG_CUDA(cudaStreamSynchronize(s));
-    if (tc_errors() != before) throw Error(DEVICE_TIMEOUT, "tensor-core projection: a bounded wait gave up");
+    if (*hfail != 0) throw Error(DEVICE_TIMEOUT, "tensor-core projection: a bounded wait gave up");
     const double2* r = reinterpret_cast<const double2*>(ws.host);
     for (int j = 0; j < k; ++j)
         for (int o = 0; o < nw; ++o) out[(size_t)o * k + j] = {r[(size_t)j * nw + o].x, r[(size_t)j * nw + o].y};
