@@ -87,15 +87,21 @@ def peaks():
 
 
 def profile_traffic():
-    """dram bytes per SpMV launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "spmv_f32_heisenberg_L28.md")
+    """DRAM bytes per SpMV launch of the Lanczos loop from the committed ncu
+    summary of the fused launch: LANCZOS_STEPS - 1 launches that read x and
+    the previous vector and write y, and the first one (no previous vector)."""
+    p = os.path.join(ROOT, "profiles", "spmv_lanczos_fused_f32_heisenberg_L28.md")
+    vals = {}
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
+            if line.startswith("traffic_bytes_per_"):
+                k, v = line.split(":")
+                vals[k.strip()] = float(v)
     except OSError:
-        pass
-    return None
+        return None
+    if "traffic_bytes_per_fused_launch" not in vals or "traffic_bytes_per_first_launch" not in vals:
+        return None
+    return ((LANCZOS_STEPS - 1) * vals["traffic_bytes_per_fused_launch"] + vals["traffic_bytes_per_first_launch"]) / LANCZOS_STEPS
 
 
 class Clocks:
@@ -331,15 +337,18 @@ def main():
     if rank != 0:
         return
     hbm_peak, peak_kind = peaks()
-    alg_bytes = 2 * DIM * BYTES_PER_ELEM_F32
+    # each launch of the loop reads x and the previous Lanczos vector and writes y
+    # (the recurrence is fused into the SpMV); the first has no previous vector
+    alg_bytes = (3 * (LANCZOS_STEPS - 1) + 2) * DIM * BYTES_PER_ELEM_F32 / LANCZOS_STEPS
     achieved = alg_bytes / spmv_s / 1e9
-    tr = profile_traffic()
     variant, _ = H.tuning(fp32=True)
+    tr = profile_traffic() if variant == "rows4" else None  # the summary covers the four-rows kernel
     kname = {"rows4": "spmv_rows_kernel<float>", "rows4_staged": "spmv_rows_kernel<float, staged>",
              "rows4_wide": "spmv_rows_kernel<float, 4 CTAs/SM>",
              "row": "spmv_fast_kernel<float>",
              "staged": "spmv_fast_kernel<float, staged>"}.get(variant, "spmv_kernel<float>")
-    out["roofline"] = {"kernel": kname + " (FP32 SpMV)", "bound": "hbm", "achieved": achieved,
+    out["roofline"] = {"kernel": kname + " (FP32 SpMV fused with the three-term recurrence)", "bound": "hbm",
+                       "achieved": achieved,
                        "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
                        "traffic": tr, "algorithmic_bytes_per_launch": alg_bytes,
                        "launch_ms": spmv_s * 1e3}

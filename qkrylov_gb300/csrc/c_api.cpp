@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 
@@ -582,23 +583,44 @@ int qkrylov_device_wait_timeouts(uint32_t* count) {
     if (*count) rc = QKRYLOV_ERROR_DEVICE_TIMEOUT;
     return rc;
 }
+constexpr int kMdotMaxVectors = 4088;  // the CUDA-core kernel's limit on k * nw (k alone at nw = 1)
 int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
                                    int method, double* out, void* stream) {
     if (!v_dev || !w_dev || !out || k < 1 || nw < 1 || nw > 4 || (method != 0 && method != 1))
         return QKRYLOV_ERROR_INVALID_ARG;
     if (method == 1 && !qkg::mdot_tc_supported(k, nw)) return QKRYLOV_ERROR_INVALID_ARG;
     if (method == 0 && (size_t)k * nw > 4088) return QKRYLOV_ERROR_INVALID_ARG;
+    if (method == 1) {  // the tensor-core kernel copies 16-byte chunks
+        for (int j = 0; j < k; ++j)
+            if (reinterpret_cast<uintptr_t>(v_dev[j]) & 15u) return QKRYLOV_ERROR_INVALID_ARG;
+        for (int o = 0; o < nw; ++o)
+            if (reinterpret_cast<uintptr_t>(w_dev[o]) & 15u) return QKRYLOV_ERROR_INVALID_ARG;
+    }
     return guarded([&] {
         cudaStream_t s = static_cast<cudaStream_t>(stream);
-        qkg::DBuf tab((size_t)k * sizeof(void*));
-        QKG_CUDA(cudaMemcpyAsync(tab.p, v_dev, (size_t)k * sizeof(void*), cudaMemcpyHostToDevice, s));
+        // one pointer table and workspace per device, kept between calls (no
+        // allocation per call); calls are serialised
+        struct Scratch {
+            qkg::DBuf tab;
+            std::unique_ptr<qkg::Workspace> ws;
+        };
+        static std::mutex mu;
+        static std::map<int, Scratch> scratch;
+        int dev = 0;
+        QKG_CUDA(cudaGetDevice(&dev));
+        std::lock_guard<std::mutex> lk(mu);
+        Scratch& sc = scratch[dev];
+        if (!sc.ws) {
+            sc.tab.alloc((size_t)kMdotMaxVectors * sizeof(void*));
+            sc.ws = std::make_unique<qkg::Workspace>(1 << 16);
+        }
+        QKG_CUDA(cudaMemcpyAsync(sc.tab.p, v_dev, (size_t)k * sizeof(void*), cudaMemcpyHostToDevice, s));
         std::vector<float2*> w(nw);
         for (int o = 0; o < nw; ++o) w[o] = const_cast<float2*>(static_cast<const float2*>(w_dev[o]));
-        qkg::Workspace ws(1 << 16);
         std::vector<cd> r((size_t)k * nw);
-        const auto* V = static_cast<const float2* const*>(tab.p);
-        if (method == 1) qkg::mdot_multi_f32_tc(V, k, w.data(), nw, n, r.data(), ws, s);
-        else qkg::mdot_multi_f32_cuda(V, k, w.data(), nw, n, r.data(), ws, s);
+        const auto* V = static_cast<const float2* const*>(sc.tab.p);
+        if (method == 1) qkg::mdot_multi_f32_tc(V, k, w.data(), nw, n, r.data(), *sc.ws, s);
+        else qkg::mdot_multi_f32_cuda(V, k, w.data(), nw, n, r.data(), *sc.ws, s);
         for (size_t i = 0; i < r.size(); ++i) {
             out[2 * i] = r[i].real();
             out[2 * i + 1] = r[i].imag();

@@ -132,7 +132,7 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, ui
 template <int NW, int LPT>
 __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const* __restrict__ V, int k,
                                                              const float2* const* __restrict__ W, uint64_t n,
-                                                             uint64_t stages_per_cta, uint32_t np, uint32_t tcols,
+                                                             uint32_t np, uint32_t tcols,
                                                              double2* __restrict__ part, int stride,
                                                              unsigned int* __restrict__ fail) {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
@@ -173,9 +173,12 @@ __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s_tmem;
 
-    const uint64_t s_begin = (uint64_t)blockIdx.x * stages_per_cta;
+    // Stages are dealt out round robin (stage s to CTA s mod gridDim.x), so the
+    // grid sweeps every vector front to back together: the pages in use at once
+    // stay few (a contiguous range per CTA touches a page per CTA and vector).
     const uint64_t total_stages = (n + 16ull * kTcKc - 1) / (16ull * kTcKc);
-    const uint64_t s_end = s_begin + stages_per_cta < total_stages ? s_begin + stages_per_cta : total_stages;
+    const uint64_t g = gridDim.x;
+    const uint32_t n_it = blockIdx.x < total_stages ? (uint32_t)((total_stages - blockIdx.x + g - 1) / g) : 0u;
     const uint32_t idesc = tc_idesc(np);
     bool ok = true;  // uniform: every thread reads s_fail after a barrier
     uint32_t chunk_fill = 0;
@@ -202,12 +205,12 @@ __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const
             out_a = load2(W[o], f0 + 16ull * (rem >> 3) + 2ull * (rem & 7u), n);
         }
     };
-    if (s_begin < s_end) load_stage(s_begin, vb, wa);
-    for (uint64_t s = s_begin; s < s_end && ok; ++s) {
-        const uint32_t it = (uint32_t)(s - s_begin), b = it & 1u;
+    if (n_it > 0) load_stage(blockIdx.x, vb, wa);
+    for (uint32_t it = 0; it < n_it && ok; ++it) {
+        const uint32_t b = it & 1u;
         unsigned char* sb = stage[b];
         float4 nb[LPT], na = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (s + 1 < s_end) load_stage(s + 1, nb, na);
+        if (it + 1 < n_it) load_stage(blockIdx.x + (uint64_t)(it + 1) * g, nb, na);
         // the MMAs that read this stage two iterations ago are complete
         if (it >= 2 && !tc_wait(bar[b], ((it - 2) >> 1) & 1u)) {
             if (lane == 0) {
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(kTcThreads) mdot_tc_kernel(const float2* const
         }
         ++chunk_fill;
         // read the accumulator out every kTcChunkStages stages and at the end
-        if (chunk_fill == (uint32_t)kTcChunkStages || s + 1 == s_end) {
+        if (chunk_fill == (uint32_t)kTcChunkStages || it + 1 == n_it) {
             if (!tc_wait(bar[b], (it >> 1) & 1u)) {
                 if (lane == 0) {
                 atomicAdd(&g_tc_errors, 1u);
@@ -354,20 +357,23 @@ void allow_tc(int lim) {
 }
 template <int LPT>
 void launch_tc(int nw, int g, size_t smem, cudaStream_t s, const float2* const* V, int k, float2* const* dw, uint64_t n,
-               uint64_t per, uint32_t np, uint32_t tcols, double2* part, unsigned int* fail) {
+               uint32_t np, uint32_t tcols, double2* part, unsigned int* fail) {
     switch (nw) {
-        case 1: mdot_tc_kernel<1, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
-        case 2: mdot_tc_kernel<2, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
-        case 3: mdot_tc_kernel<3, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
-        default: mdot_tc_kernel<4, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, per, np, tcols, part, g, fail); break;
+        case 1: mdot_tc_kernel<1, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, np, tcols, part, g, fail); break;
+        case 2: mdot_tc_kernel<2, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, np, tcols, part, g, fail); break;
+        case 3: mdot_tc_kernel<3, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, np, tcols, part, g, fail); break;
+        default: mdot_tc_kernel<4, LPT><<<g, kTcThreads, smem, s>>>(V, k, dw, n, np, tcols, part, g, fail); break;
     }
 }
 
-// CTAs of the kernel for (nw, lpt) resident on the whole GPU at this shared memory
+// CTAs of the kernel for (nw, lpt) resident on the whole GPU at this shared
+// memory and tensor-memory width, from the kernel's registers, the SM's shared
+// memory (1 KB reserved per CTA) and the 512 tensor-memory columns of an SM
 // (the caller caches it).
-int tc_resident(int dev, int nw, int lpt, size_t smem) {
-    int sms = 0, per = 0;
+int tc_resident(int dev, int nw, int lpt, size_t smem, uint32_t tcols) {
+    int sms = 0, smem_sm = 0;
     QKG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    QKG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     const void* f = nullptr;
     auto pick = [&](auto k1, auto k2, auto k3, auto k4) {
         f = nw == 1 ? (const void*)k1 : nw == 2 ? (const void*)k2 : nw == 3 ? (const void*)k3 : (const void*)k4;
@@ -375,8 +381,15 @@ int tc_resident(int dev, int nw, int lpt, size_t smem) {
     if (lpt == 2) pick(mdot_tc_kernel<1, 2>, mdot_tc_kernel<2, 2>, mdot_tc_kernel<3, 2>, mdot_tc_kernel<4, 2>);
     else if (lpt == 4) pick(mdot_tc_kernel<1, 4>, mdot_tc_kernel<2, 4>, mdot_tc_kernel<3, 4>, mdot_tc_kernel<4, 4>);
     else pick(mdot_tc_kernel<1, 8>, mdot_tc_kernel<2, 8>, mdot_tc_kernel<3, 8>, mdot_tc_kernel<4, 8>);
-    QKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kTcThreads, smem));
-    return std::max(1, per) * std::max(1, sms);
+    cudaFuncAttributes fa{};
+    QKG_CUDA(cudaFuncGetAttributes(&fa, f));
+    const int warp_regs = ((std::max(fa.numRegs, 1) * 32 + 255) / 256) * 256;  // allocated per warp in 256s
+    const int by_regs = 65536 / (warp_regs * (kTcThreads / 32));
+    const int by_smem = smem_sm / (int)(smem + fa.sharedSizeBytes + 1024);
+    const int by_tmem = 512 / (int)tcols;
+    const int by_threads = 2048 / kTcThreads;
+    const int per = std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_tmem, by_threads)));
+    return per * std::max(1, sms);
 }
 
 }  // namespace
@@ -424,7 +437,7 @@ void mdot_multi_f32_tc(const float2* const* V, int k, float2* const* W, int nw, 
             c[0] = 1;
         }
         int& r = c[1 + 8 * (nw - 1) + (int)(np / 16) - 1];
-        if (!r) r = tc_resident(dev, nw, lpt, smem);
+        if (!r) r = tc_resident(dev, nw, lpt, smem, tcols);
         resident = r;
     }
     // Host-side scratch in the pinned result slots: the W pointer table (copied in
@@ -442,13 +455,12 @@ void mdot_multi_f32_tc(const float2* const* V, int k, float2* const* W, int nw, 
     // one wave: as many CTAs as can be resident at once
     const uint64_t want =
         std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)resident, ws.cap_partials / ((size_t)k * nw)));
-    const uint64_t per = std::max<uint64_t>(1, (total + want - 1) / want);
-    const int g = (int)std::max<uint64_t>(1, (total + per - 1) / per);
+    const int g = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, total));
     QKG_REQUIRE((size_t)g * k * nw <= ws.cap_partials, "tensor-core projections: workspace too small");
     double2* part = ws.partial.as<double2>();
-    if (lpt == 2) launch_tc<2>(nw, g, smem, s, V, k, dw, n, per, np, tcols, part, dfail);
-    else if (lpt == 4) launch_tc<4>(nw, g, smem, s, V, k, dw, n, per, np, tcols, part, dfail);
-    else launch_tc<8>(nw, g, smem, s, V, k, dw, n, per, np, tcols, part, dfail);
+    if (lpt == 2) launch_tc<2>(nw, g, smem, s, V, k, dw, n, np, tcols, part, dfail);
+    else if (lpt == 4) launch_tc<4>(nw, g, smem, s, V, k, dw, n, np, tcols, part, dfail);
+    else launch_tc<8>(nw, g, smem, s, V, k, dw, n, np, tcols, part, dfail);
     QKG_LAUNCHED();
     tc_finish_kernel<<<k * nw, 256, 0, s>>>(part, g, g, ws.result.as<double2>());
     QKG_LAUNCHED();

@@ -6,6 +6,8 @@ profiles are taken with).
     python -m qkrylov_gb300.timing --model hubbard --L 14 --davidson 4 --iters 14 [--projection tensor]
 
     python -m qkrylov_gb300.timing --peaks
+    python -m qkrylov_gb300.timing --mdot 32 --nw 4 --n 50000000 --reps 20
+    python -m qkrylov_gb300.timing --L 28 --lanczos 8 [--mode 4]
 
 The second form runs the batched Lanczos on every Sz sector of the chain (or
 the Sz = 0 sector alone with ``--sz0-only``) with ``--block`` Philox start
@@ -14,7 +16,15 @@ Davidson solver for the ``--davidson`` lowest states (subspace 32, mixed form
 unless ``--precision fp64``) for ``--iters`` iterations, twice, and reports
 the seconds per iteration of the second run.  ``--peaks`` compiles and runs
 ``peaks.cu`` (FP64/FP32 FMA rates, L2 and DRAM read bandwidth, scattered
-8-byte reads from shared memory and L1) and prints its JSON line.
+8-byte reads from shared memory and L1) and prints its JSON line.  ``--mdot K``
+times the projections <V_j, W_o> of K FP32 vectors against ``--nw`` others of
+``--n`` complex elements (qkrylov_vector_mdot_device_f32) with both kernels,
+the compensated CUDA-core one and the tcgen05 one, and reports microseconds per
+call and the algorithmic bandwidth (every vector read once).  ``--lanczos N``
+runs N steps of the mixed Lanczos (qkrylov_lanczos_fixed_steps) on the
+Heisenberg chain, twice, and reports the mean time of its SpMV launches, each
+fused with the three-term recurrence (reads x and the previous Lanczos vector,
+writes y): the Lanczos step's SpMV on a few vectors instead of the bench's 200.
 
 Builds the Hamiltonian (Heisenberg chain ``Sz Sz + 0.5 (S+ S- + S- S+)`` per
 bond, or Fermi-Hubbard chain ``-t c^dag c`` hopping per spin and direction plus
@@ -69,6 +79,10 @@ def main():
     p.add_argument("--davidson", type=int, default=0, help="states for a Davidson run (0: SpMV timing)")
     p.add_argument("--iters", type=int, default=14, help="Davidson iterations")
     p.add_argument("--peaks", action="store_true", help="FMA / L2 / DRAM / gather throughput probes")
+    p.add_argument("--lanczos", type=int, default=0, help="mixed Lanczos steps (0: none)")
+    p.add_argument("--mdot", type=int, default=0, help="vectors of a projection timing (0: none)")
+    p.add_argument("--nw", type=int, default=4, help="right-hand vectors of the projection timing")
+    p.add_argument("--n", type=int, default=50_000_000, help="vector length of the projection timing")
     p.add_argument("--projection", choices=["cuda", "tensor"], default="cuda",
                    help="kernel of the mixed Davidson's projections")
     a = p.parse_args()
@@ -78,6 +92,10 @@ def main():
         return block(a)
     if a.davidson:
         return davidson(a)
+    if a.mdot:
+        return mdot(a)
+    if a.lanczos:
+        return lanczos(a)
     build = heisenberg_chain if a.model == "heisenberg" else hubbard_chain
     basis, site, ops = build(a.L, not a.obc)
     t0 = time.perf_counter()
@@ -132,6 +150,49 @@ def davidson(a):
                       "projection": a.projection, "iterations": r.iterations, "s_per_iteration": r.seconds / max(1, r.iterations),
                       "eigenvalues": [float(e) for e in r.eigenvalues],
                       "residuals": [float(e) for e in r.residuals]}), flush=True)
+
+
+def lanczos(a):
+    H = qk.MatrixFreeHamiltonian(*heisenberg_chain(a.L, not a.obc))
+    if a.mode:  # a fixed variant (a profiler's slow-down can change the autotuner's choice)
+        H.select_kernel(mode=a.mode)
+    for _ in range(2):  # the second run is reported
+        r = qk.lanczos_fixed_steps(H, a.lanczos, seed=1, mixed=True)
+    n = H.dimension
+    ms = 1e3 * r.seconds_spmv / max(1, r.spmv_calls)
+    variant, _ = H.tuning(fp32=True)
+    print(json.dumps({"model": "heisenberg", "L": a.L, "dim": n, "steps": a.lanczos, "spmv_calls": r.spmv_calls,
+                      "spmv_ms": ms, "alg_bytes_per_launch": 3 * n * 8, "alg_GBs": 3 * n * 8 / ms / 1e6,
+                      "variant": variant, "energy": r.energy}), flush=True)
+
+
+def mdot(a):
+    import ctypes
+    import torch
+    k, nw, n = a.mdot, a.nw, a.n
+    g = torch.Generator(device="cuda").manual_seed(1)
+    V = [torch.randn(n, dtype=torch.complex64, device="cuda", generator=g) for _ in range(k)]
+    W = [torch.randn(n, dtype=torch.complex64, device="cuda", generator=g) for _ in range(nw)]
+    va = (ctypes.c_void_p * k)(*[v.data_ptr() for v in V])
+    wa = (ctypes.c_void_p * nw)(*[w.data_ptr() for w in W])
+    out = (ctypes.c_double * (2 * k * nw))()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    res = {"k": k, "nw": nw, "n": n, "bytes_per_call": (k + nw) * n * 8}
+    vals = {}
+    for name, method in (("cuda", 0), ("tensor", 1)):
+        call = lambda: qk.lib().qkrylov_vector_mdot_device_f32(va, k, wa, nw, n, method, out, stream)
+        for _ in range(3):
+            assert call() == 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.reps):
+            call()  # returns after the result is on the host
+        t = (time.perf_counter() - t0) / a.reps
+        vals[name] = list(out)
+        res[name + "_us"] = round(t * 1e6, 1)
+        res[name + "_GBs"] = round(res["bytes_per_call"] / t / 1e9, 1)
+    res["max_rel_diff"] = max(abs(x - y) for x, y in zip(vals["cuda"], vals["tensor"])) / max(map(abs, vals["cuda"]))
+    print(json.dumps(res), flush=True)
 
 
 if __name__ == "__main__":

@@ -40,7 +40,9 @@ def _mdot(qk, dv, dw, n, method):
     return rc, out.view(np.complex128).reshape(nw, k)
 
 
-@pytest.mark.parametrize("n,k,nw", [(1_000_003, 36, 4), (4097, 1, 1), (5, 3, 2), (70_000, 128, 3), (300_000, 17, 4)])
+# (the ring depth of the tensor-core kernel runs from 14 stages at k <= 16 to 1 at k > 96)
+@pytest.mark.parametrize("n,k,nw", [(1_000_003, 36, 4), (4097, 1, 1), (5, 3, 2), (70_000, 128, 3), (300_000, 17, 4),
+                                    (2_000_001, 64, 4), (123_457, 100, 2), (33, 8, 1)])
 def test_projection_kernels_against_fp64(qk, n, k, nw):
     cudart = _cudart()
     rng = np.random.default_rng(n + k)
@@ -76,6 +78,9 @@ def test_projection_kernel_arguments(qk):
     assert L.qkrylov_vector_mdot_device_f32(va, 129, va, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG  # k > 128
     assert L.qkrylov_vector_mdot_device_f32(va, 1, va, 5, 8, 1, dp, None) == qk.ERROR_INVALID_ARG    # nw > 4
     assert L.qkrylov_vector_mdot_device_f32(va, 1, va, 1, 8, 2, dp, None) == qk.ERROR_INVALID_ARG    # method
+    v8 = (ctypes.c_void_p * 1)(24)  # off the 16-byte grid: the tensor-core kernel refuses it
+    assert L.qkrylov_vector_mdot_device_f32(v8, 1, va, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_mdot_device_f32(va, 1, v8, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_set_projection_kernel(7) == qk.ERROR_INVALID_ARG
 
 
