@@ -229,6 +229,17 @@ int qkrylov_lanczos_ground_state_mixed(qkrylov_hamiltonian_h h, int maxiter, dou
 int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed,
                                 const double* v0_complex, qkrylov_lanczos_result_f64_t* result,
                                 double* eigenvector_complex);
+/* Lowest Ritz values of the Lanczos tridiagonal after n_steps steps from the
+ * seeded Philox start of qkrylov_lanczos_fixed_steps (mixed: 0 FP64 with full
+ * reorthogonalisation, 1 the mixed form, 2 FP64 with selective
+ * reorthogonalisation): values[0..*n_out-1] ascending, *n_out = min(n_values,
+ * steps run); selective reorthogonalisation guards the converged Ritz vectors
+ * among the min(n_values, 4) lowest (the ground-state entry points guard the
+ * lowest only), and *n_locked (may be NULL) = how many it held at the end (0
+ * with full reorthogonalisation).  No counterpart in the reference, whose Lanczos reports
+ * the ground state only (src/solvers/lanczos.cpp:175). */
+int qkrylov_lanczos_ritz_values(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed, int n_values,
+                                double* values, int* n_out, int* n_locked);
 
 /* Number of kernels this library has launched so far in the process. */
 uint64_t qkrylov_kernel_launches(void);

@@ -118,6 +118,7 @@ _SIGS = {
     "qkrylov_vector_mdot_device_f32": (_i, [_c.POINTER(_c.c_void_p), _i, _c.POINTER(_c.c_void_p), _i, _c.c_uint64, _i,
                                             _dp, _vp]),
     "qkrylov_set_projection_kernel": (_i, [_i]),
+    "qkrylov_lanczos_ritz_values": (_i, [_vp, _i, _c.c_uint64, _i, _i, _dp, _ip, _ip]),
     "qkrylov_debug_live_allocations": (_c.c_int64, []),
     "qkrylov_debug_device_wait_probe": (_i, [_c.c_int64]),
     "qkrylov_vector_dot_device_f64": (_i, [_vp, _vp, _u64, _dp, _vp]),
@@ -505,6 +506,18 @@ def lanczos_fixed_steps(H, n_steps, seed=0, mixed=True, v0=None, eigenvector_out
     m = 1 if mixed else (2 if selective else 0)
     _check(lib().qkrylov_lanczos_fixed_steps(H._h, int(n_steps), int(seed), m, v0p, _c.byref(r), evp))
     return r
+
+
+def lanczos_ritz_values(H, n_steps, n_values, seed=0, mixed=True, selective=False):
+    """Lowest n_values Ritz values of the tridiagonal after n_steps Lanczos
+    steps from a seeded Philox start (the run of lanczos_fixed_steps), and the
+    number of converged Ritz vectors selective reorthogonalisation held."""
+    vals = _np.zeros(int(n_values))
+    m, locked = _c.c_int(), _c.c_int()
+    mode = 1 if mixed else (2 if selective else 0)
+    _check(lib().qkrylov_lanczos_ritz_values(H._h, int(n_steps), int(seed), mode, int(n_values), _dptr(vals),
+                                             _c.byref(m), _c.byref(locked)))
+    return vals[:m.value], int(locked.value)
 
 
 def kernel_launches():

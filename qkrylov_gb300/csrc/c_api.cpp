@@ -573,6 +573,30 @@ int qkrylov_lanczos_fixed_steps(qkrylov_hamiltonian_h h, int n_steps, uint64_t s
     });
 }
 
+int qkrylov_lanczos_ritz_values(qkrylov_hamiltonian_h h, int n_steps, uint64_t seed, int mixed, int n_values,
+                                double* values, int* n_out, int* n_locked) {
+    if (!h || !h->ptr || !values || !n_out || n_steps <= 0 || n_values <= 0 || mixed < 0 || mixed > 2)
+        return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded_solve(h, [&] {
+        set_device(h);
+        qkg::LanczosOpts o;
+        o.maxiter = n_steps;
+        o.fixed_steps = true;
+        o.selective = (mixed == 2);
+        o.device_start = true;
+        o.seed = seed;
+        o.ritz_guard = std::min(n_values, qkg::kMaxRitzLocked);  // the wanted end of the spectrum
+        const auto res = mixed == 1 ? qkg::lanczos_mixed(*h->ptr, o) : qkg::lanczos_f64(*h->ptr, o);
+        std::vector<double> d, z;
+        qkg::tridiag_eig(res.alphas.data(), res.betas.data(), (int)res.alphas.size(), d, {}, z);
+        std::sort(d.begin(), d.end());
+        const int m = std::min<int>(n_values, (int)d.size());
+        std::copy(d.begin(), d.begin() + m, values);
+        *n_out = m;
+        if (n_locked) *n_locked = res.n_ritz_locked;
+    });
+}
+
 uint64_t qkrylov_kernel_launches(void) { return qkg::launch_count(); }
 
 int qkrylov_device_wait_timeouts(uint32_t* count) {

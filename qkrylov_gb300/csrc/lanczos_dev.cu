@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <type_traits>
 
 namespace qkg {
 
@@ -34,11 +35,16 @@ constexpr int kTimedSteps = 8;  // steps launched one by one with an SpMV timer 
 constexpr int kInFlight = 6;    // steps the host lets the GPU run ahead of its checks
 constexpr double kOrthTol = 3.4526698300124393e-4;  // sqrt(2^-23): FP32 semiorthogonality level
 
+constexpr int kMaxPsi = kMaxRitzLocked;  // converged Ritz vectors held for selective reorthogonalisation
+
 struct LzState {
     int k;
-    int orth;               // this step's correction along the Ritz vector is applied
+    int orth;               // this step's correction along the Ritz vectors is applied
     double a, b;            // update coefficients of the current step
-    double pre, pim;        // projection on the Ritz vector (selective reorthogonalisation)
+    double pre[kMaxPsi], pim[kMaxPsi];  // projections on the Ritz vectors (selective reorthogonalisation)
+};
+struct PsiTab {
+    const float2* p[kMaxPsi];
 };
 
 __device__ __forceinline__ void ff_acc(float& hi, float& lo, float a, float b) {
@@ -103,13 +109,15 @@ __global__ void lz_alpha_kernel(const double2* __restrict__ apart, int nparts, L
 }
 
 // One element of the update w -= a v + b v_prev with its ||w||^2 (and, with
-// psi, <psi, w>) contributions.
+// NP Ritz vectors psi_p, the <psi_p, w>) contributions.
+template <int NP>
 struct UpdAcc {
-    float hi = 0.f, lo = 0.f, rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    float hi = 0.f, lo = 0.f;
+    float rh[NP > 0 ? NP : 1] = {}, rl[NP > 0 ? NP : 1] = {}, ih[NP > 0 ? NP : 1] = {}, il[NP > 0 ? NP : 1] = {};
 };
-template <bool PROJ>
-__device__ __forceinline__ float2 upd_elem(float2 x, float2 c, float2 d, float2 p, float a, float b, bool has_prev,
-                                           UpdAcc& s) {
+template <int NP>
+__device__ __forceinline__ float2 upd_elem(float2 x, float2 c, float2 d, const float2 (&p)[NP > 0 ? NP : 1], float a,
+                                           float b, bool has_prev, UpdAcc<NP>& s) {
     x.x = fmaf(-a, c.x, x.x);
     x.y = fmaf(-a, c.y, x.y);
     if (has_prev) {
@@ -118,86 +126,115 @@ __device__ __forceinline__ float2 upd_elem(float2 x, float2 c, float2 d, float2 
     }
     ff_acc(s.hi, s.lo, x.x, x.x);
     ff_acc(s.hi, s.lo, x.y, x.y);
-    if (PROJ) {
-        ff_acc(s.rh, s.rl, p.x, x.x);
-        ff_acc(s.rh, s.rl, p.y, x.y);
-        ff_acc(s.ih, s.il, p.x, x.y);
-        ff_acc(s.ih, s.il, -p.y, x.x);
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        ff_acc(s.rh[q], s.rl[q], p[q].x, x.x);
+        ff_acc(s.rh[q], s.rl[q], p[q].y, x.y);
+        ff_acc(s.ih[q], s.il[q], p[q].x, x.y);
+        ff_acc(s.ih[q], s.il[q], -p[q].y, x.x);
     }
     return x;
 }
 
 // w -= a v + b v_prev in place (b = 0: the SpMV applied the previous-vector
-// term, and v_prev is not read), ||w||^2 partials (and <psi, w> partials with
-// PROJ, for selective reorthogonalisation): two elements per thread and
-// iteration with 16-byte accesses (the Krylov vectors are 256-byte aligned).
-template <bool PROJ>
+// term, and v_prev is not read), ||w||^2 partials (and the <psi_q, w> partials
+// of the NP Ritz vectors, for selective reorthogonalisation): two elements per
+// thread and iteration with 16-byte accesses (the Krylov vectors are 256-byte
+// aligned).  ppart[q * gridDim.x + block] holds Ritz vector q's partial.
+template <int NP>
 __global__ void lz_update_t(void* const* __restrict__ vtab, const LzState* __restrict__ st, uint64_t n,
-                            const float2* __restrict__ psi, double2* __restrict__ bpart,
-                            double2* __restrict__ ppart) {
+                            const PsiTab psi, double2* __restrict__ bpart, double2* __restrict__ ppart) {
     const int k = st->k;
     float2* __restrict__ w = static_cast<float2*>(vtab[k + 1]);
     const float2* __restrict__ v = static_cast<const float2*>(vtab[k]);
     const float a = (float)st->a, b = (float)st->b;
     const bool has_prev = k > 0 && b != 0.f;
     const float2* __restrict__ vp = has_prev ? static_cast<const float2*>(vtab[k - 1]) : v;
-    UpdAcc s;
+    UpdAcc<NP> s;
+    constexpr int NQ = NP > 0 ? NP : 1;
     const uint64_t n2 = n / 2, step = (uint64_t)gridDim.x * blockDim.x;
-    const float2 zero = make_float2(0.f, 0.f);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n2; i += step) {
         const float4 x4 = reinterpret_cast<const float4*>(w)[i];
         const float4 c4 = reinterpret_cast<const float4*>(v)[i];
         float4 d4 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (has_prev) d4 = reinterpret_cast<const float4*>(vp)[i];
-        float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (PROJ) p4 = reinterpret_cast<const float4*>(psi)[i];
-        const float2 y0 = upd_elem<PROJ>(make_float2(x4.x, x4.y), make_float2(c4.x, c4.y), make_float2(d4.x, d4.y),
-                                         make_float2(p4.x, p4.y), a, b, has_prev, s);
-        const float2 y1 = upd_elem<PROJ>(make_float2(x4.z, x4.w), make_float2(c4.z, c4.w), make_float2(d4.z, d4.w),
-                                         make_float2(p4.z, p4.w), a, b, has_prev, s);
+        float2 p0[NQ], p1[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (q < NP) p4 = reinterpret_cast<const float4*>(psi.p[q])[i];
+            p0[q] = make_float2(p4.x, p4.y);
+            p1[q] = make_float2(p4.z, p4.w);
+        }
+        const float2 y0 = upd_elem<NP>(make_float2(x4.x, x4.y), make_float2(c4.x, c4.y), make_float2(d4.x, d4.y),
+                                       p0, a, b, has_prev, s);
+        const float2 y1 = upd_elem<NP>(make_float2(x4.z, x4.w), make_float2(c4.z, c4.w), make_float2(d4.z, d4.w),
+                                       p1, a, b, has_prev, s);
         reinterpret_cast<float4*>(w)[i] = make_float4(y0.x, y0.y, y1.x, y1.y);
     }
-    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
-        w[n - 1] = upd_elem<PROJ>(w[n - 1], v[n - 1], vp[n - 1], PROJ ? psi[n - 1] : zero, a, b, has_prev, s);
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        float2 pl[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) pl[q] = q < NP ? psi.p[q][n - 1] : make_float2(0.f, 0.f);
+        w[n - 1] = upd_elem<NP>(w[n - 1], v[n - 1], vp[n - 1], pl, a, b, has_prev, s);
+    }
     const double2 t = bsum2((double)s.hi + (double)s.lo, 0.0);
-    if (PROJ) {
-        const double2 q = bsum2((double)s.rh + (double)s.rl, (double)s.ih + (double)s.il);
-        if (threadIdx.x == 0) ppart[blockIdx.x] = q;
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        const double2 r = bsum2((double)s.rh[q] + (double)s.rl[q], (double)s.ih[q] + (double)s.il[q]);
+        if (threadIdx.x == 0) ppart[(size_t)q * gridDim.x + blockIdx.x] = r;
     }
     if (threadIdx.x == 0) bpart[blockIdx.x] = t;
 }
 
-// c = <psi, W>; the correction is applied only when |c| exceeds orth_tol ||W||
-// (components below the square root of the working precision are harmless,
-// Parlett & Scott 1979), so most steps skip the extra pass over W.
+// c_q = <psi_q, W> for the NP Ritz vectors; the correction is applied only
+// when some |c_q| exceeds orth_tol ||W|| (components below the square root of
+// the working precision are harmless, Parlett & Scott 1979), so most steps skip
+// the extra pass over W.
+template <int NP>
 __global__ void lz_proj_finish_kernel(const double2* __restrict__ ppart, const double2* __restrict__ bpart,
                                       int nparts, LzState* st, double orth_tol) {
-    double r = 0.0, i = 0.0, w2 = 0.0;
-    for (int j = threadIdx.x; j < nparts; j += blockDim.x) {
-        r += ppart[j].x;
-        i += ppart[j].y;
-        w2 += bpart[j].x;
-    }
-    const double2 t = bsum2(r, i);
+    double w2 = 0.0;
+    for (int j = threadIdx.x; j < nparts; j += blockDim.x) w2 += bpart[j].x;
     const double2 u = bsum2(w2, 0.0);
-    if (threadIdx.x == 0) {
-        st->pre = t.x;
-        st->pim = t.y;
-        st->orth = (t.x * t.x + t.y * t.y) > orth_tol * orth_tol * u.x ? 1 : 0;
+    int orth = 0;
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        double r = 0.0, i = 0.0;
+        for (int j = threadIdx.x; j < nparts; j += blockDim.x) {
+            r += ppart[(size_t)q * nparts + j].x;
+            i += ppart[(size_t)q * nparts + j].y;
+        }
+        const double2 t = bsum2(r, i);
+        if (threadIdx.x == 0) {
+            st->pre[q] = t.x;
+            st->pim[q] = t.y;
+            orth |= (t.x * t.x + t.y * t.y) > orth_tol * orth_tol * u.x ? 1 : 0;
+        }
     }
+    if (threadIdx.x == 0) st->orth = orth;
 }
-// W -= c psi with c = <psi, W>; |W|^2 partials.
-__global__ void lz_orth_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st,
-                               const float2* __restrict__ psi, uint64_t n, double2* __restrict__ bpart) {
+// W -= sum_q c_q psi_q with c_q = <psi_q, W>; |W|^2 partials.
+template <int NP>
+__global__ void lz_orth_kernel(void* const* __restrict__ vtab, const LzState* __restrict__ st, const PsiTab psi,
+                               uint64_t n, double2* __restrict__ bpart) {
     if (!st->orth) return;  // bpart keeps the partials of the unchanged W
     float2* __restrict__ w = static_cast<float2*>(vtab[st->k + 1]);
-    const float cr = (float)st->pre, ci = (float)st->pim;
+    float cr[NP], ci[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        cr[q] = (float)st->pre[q];
+        ci[q] = (float)st->pim[q];
+    }
     float hi = 0.f, lo = 0.f;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const float2 p = psi[i];
         float2 x = w[i];
-        x.x -= cr * p.x - ci * p.y;
-        x.y -= cr * p.y + ci * p.x;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            const float2 p = psi.p[q][i];
+            x.x -= cr[q] * p.x - ci[q] * p.y;
+            x.y -= cr[q] * p.y + ci[q] * p.x;
+        }
         w[i] = x;
         ff_acc(hi, lo, x.x, x.x);
         ff_acc(hi, lo, x.y, x.y);
@@ -262,11 +299,11 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     // vectors start on 256-byte boundaries (a warp's 32 consecutive rows then
     // cover whole 128-byte lines)
     const uint64_t stride = (n + 31) / 32 * 32;
-    // workspace: nmax + 1 Krylov vectors, then psi (FP32), the Ritz vector
-    // (FP32), the refined Ritz vector and its residual (FP64); the FP64 slots
-    // also stage a caller's start vector, psi and the FP32 Ritz slot together
-    // the reference-order copy of the eigenvector
-    const size_t need = (size_t)(nmax + 1 + 6) * stride * sizeof(float2);
+    // workspace: nmax + 1 Krylov vectors, then kMaxPsi Ritz vectors psi (FP32),
+    // the Ritz vector (FP32), the refined Ritz vector and its residual (FP64);
+    // the FP64 slots also stage a caller's start vector, the first two psi
+    // slots the reference-order copy of the eigenvector
+    const size_t need = (size_t)(nmax + 1 + kMaxPsi + 5) * stride * sizeof(float2);
     if (H.workspace_bytes() < need) {
         H.release_workspace();
         size_t fr = 0, tot = 0;
@@ -280,14 +317,14 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     std::vector<void*> vptr;
     for (int i = 0; i <= nmax; ++i) vptr.push_back(V.as<float2>() + (size_t)i * stride);
     float2* const psi_p = V.as<float2>() + (size_t)(nmax + 1) * stride;
-    float2* const r32_p = psi_p + stride;
+    float2* const r32_p = psi_p + (size_t)kMaxPsi * stride;
     double2* const r64_p = reinterpret_cast<double2*>(r32_p + stride);
     double2* const h64_p = r64_p + stride;
     DBuf vtab((nmax + 1) * sizeof(void*));
     QKG_CUDA(cudaMemcpy(vtab.p, vptr.data(), vptr.size() * sizeof(void*), cudaMemcpyHostToDevice));
     DBuf state(sizeof(LzState)), alpha((nmax + 2) * 8), beta((nmax + 2) * 8), sig((nmax + 2) * 8);
     DBuf apart(std::max<size_t>(1, H.lanczos_parts()) * sizeof(double2)), bpart(kUpdGrid * sizeof(double2)),
-        ppart(kUpdGrid * sizeof(double2));
+        ppart((size_t)kMaxPsi * kUpdGrid * sizeof(double2)), psitab(kMaxPsi * sizeof(float2*));
     Mapped ah(nmax + 2), bh(nmax + 2);
     DBuf part2(kAlphaBlocks * sizeof(double)), arrived(sizeof(unsigned int));
     QKG_CUDA(cudaMemsetAsync(arrived.p, 0, sizeof(unsigned int), st));
@@ -334,8 +371,10 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     hooks.op = lzop.as<LzOperands>();
     hooks.apart = apart.as<double2>();
     const int nparts = (int)H.lanczos_parts();
-    float2* psi = nullptr;  // selective reorthogonalisation vector (once active)
-    auto enqueue_step = [&](bool so, LaunchTimer* timer) {
+    PsiTab psi{};   // converged Ritz vectors (selective reorthogonalisation)
+    int npsi = 0;   // how many are held
+    std::vector<double> locked;  // their Ritz values
+    auto enqueue_step = [&](int np, LaunchTimer* timer) {
         if (timer) timer->start();
         H.apply_lanczos_f32(hooks, st);
         if (timer) timer->stop();
@@ -343,46 +382,58 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
                                                      alpha.as<double>(), beta.as<double>(), sig.as<double>(), ah.d,
                                                      part2.as<double>(), arrived.as<unsigned int>());
         QKG_LAUNCHED();
-        if (!so) {
-            lz_update_t<false><<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
-                                                        nullptr, bpart.as<double2>(), nullptr);
+        void* const* vt = static_cast<void* const*>(vtab.p);
+        auto sel = [&](auto npc) {
+            constexpr int NP = decltype(npc)::value;
+            lz_update_t<NP><<<kUpdGrid, kT, 0, st>>>(vt, state.as<LzState>(), n, psi, bpart.as<double2>(),
+                                                     ppart.as<double2>());
             QKG_LAUNCHED();
-        } else {
-            lz_update_t<true><<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(), n,
-                                                       psi, bpart.as<double2>(), ppart.as<double2>());
-            QKG_LAUNCHED();
-            lz_proj_finish_kernel<<<1, kT, 0, st>>>(ppart.as<double2>(), bpart.as<double2>(), kUpdGrid,
-                                                    state.as<LzState>(), kOrthTol);
-            QKG_LAUNCHED();
-            lz_orth_kernel<<<kUpdGrid, kT, 0, st>>>(static_cast<void* const*>(vtab.p), state.as<LzState>(),
-                                                    psi, n, bpart.as<double2>());
-            QKG_LAUNCHED();
+            if constexpr (NP > 0) {
+                lz_proj_finish_kernel<NP><<<1, kT, 0, st>>>(ppart.as<double2>(), bpart.as<double2>(), kUpdGrid,
+                                                            state.as<LzState>(), kOrthTol);
+                QKG_LAUNCHED();
+                lz_orth_kernel<NP><<<kUpdGrid, kT, 0, st>>>(vt, state.as<LzState>(), psi, n, bpart.as<double2>());
+                QKG_LAUNCHED();
+            }
+        };
+        switch (np) {
+            case 0: sel(std::integral_constant<int, 0>{}); break;
+            case 1: sel(std::integral_constant<int, 1>{}); break;
+            case 2: sel(std::integral_constant<int, 2>{}); break;
+            case 3: sel(std::integral_constant<int, 3>{}); break;
+            default: sel(std::integral_constant<int, 4>{}); break;
         }
         lz_beta_kernel<<<1, kT, 0, st>>>(bpart.as<double2>(), kUpdGrid, state.as<LzState>(), beta.as<double>(),
                                          sig.as<double>(), bh.d, static_cast<void* const*>(vtab.p), nmax,
                                          lzop.as<LzOperands>());
         QKG_LAUNCHED();
     };
-    int kernels_plain = 0, kernels_so = 0;  // kernels per step graph, counted at capture
-    auto capture = [&](bool so) {
+    int kernels[kMaxPsi + 1] = {};  // kernels per step graph (by Ritz vectors held), counted at capture
+    auto capture = [&](int np) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
         const uint64_t c0 = launch_count();
         QKG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(so, nullptr);
+        enqueue_step(np, nullptr);
         QKG_CUDA(cudaStreamEndCapture(st, &g));
         const int64_t captured = (int64_t)(launch_count() - c0);
         add_launches(-captured);
-        (so ? kernels_so : kernels_plain) = (int)captured;  // kernels per replay
+        kernels[np] = (int)captured;  // kernels per replay
         QKG_CUDA(cudaGraphInstantiate(&ge, g, 0));
         QKG_CUDA(cudaGraphDestroy(g));
         return ge;
     };
-    cudaGraphExec_t g_plain = nullptr, g_so = nullptr;
+    cudaGraphExec_t graphs[kMaxPsi + 1] = {};
+    auto destroy_graphs = [&] {
+        for (auto& g : graphs)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    };
     std::vector<cudaEvent_t> ev(kInFlight + 2);
     for (auto& e : ev) QKG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 
-    bool so_active = false;
     int stop_at = -1;       // last accepted step (inclusive)
     bool converged = false;
     double e_old = 1e100;
@@ -400,46 +451,56 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
                 const double e = tridiag_lowest(a.data(), bb.data(), j + 1);
                 if (!o.fixed_steps && std::abs(e - e_old) < o.tol) { converged = true; stop_at = j; return; }
                 e_old = e;
-                if (!so_active && j + 1 >= 4) {
-                    std::vector<double> d, z;
-                    tridiag_eig(a.data(), bb.data(), j + 1, d, {j}, z);
-                    int mi = 0;
-                    for (int q = 1; q <= j; ++q) if (d[q] < d[mi]) mi = q;
-                    double tn = 0.0;
-                    for (double x : d) tn = std::max(tn, std::abs(x));
-                    if (b * std::abs(z[mi]) <= so_tol * tn) {
-                        // Ritz vector of T_j from v_0..v_j = sig_i V_i (sig_0 = 1, sig_{i+1} = 1/beta_i)
+                if (j + 1 >= 4) {
+                    // Parlett-Scott: lock the Ritz vectors of newly converged low Ritz values
+                    for (double theta : ritz_to_lock(a.data(), bb.data(), j + 1, b, so_tol, locked, o.ritz_guard)) {
+                        if (npsi >= kMaxPsi) break;
                         std::vector<double> s;
-                        tridiag_ground(a.data(), bb.data(), j + 1, s);
+                        if (!tridiag_vector(a.data(), bb.data(), j + 1, theta, s)) continue;
+                        // Ritz vector of T_j from v_0..v_j = sig_i V_i (sig_0 = 1, sig_{i+1} = 1/beta_i)
                         std::vector<cd> c(j + 1);
                         double sg = 1.0;
                         for (int i = 0; i <= j; ++i) {
                             c[i] = s[i] * sg;
                             sg = 1.0 / bh.h[i];
                         }
-                        psi = psi_p;
-                        QKG_CUDA(cudaMemsetAsync(psi, 0, n * sizeof(float2), st));
-                        mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), j + 1, c.data(), psi,
-                                     n, ws, st);
-                        const double pn = std::sqrt(nrm2sq_f32(psi, n, ws, st));
-                        scal_f32(1.0 / pn, psi, n, st);
-                        so_active = true;
+                        float2* p = psi_p + (size_t)npsi * stride;
+                        QKG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(float2), st));
+                        mcombine_f32(reinterpret_cast<const float2* const*>(vtab.p), j + 1, c.data(), p, n, ws, st);
+                        double pn = std::sqrt(nrm2sq_f32(p, n, ws, st));
+                        if (!(pn > 0.0)) continue;
+                        scal_f32(1.0 / pn, p, n, st);
+                        if (npsi > 0) {  // orthonormal to the Ritz vectors already held (two passes)
+                            const auto* pt = static_cast<const float2* const*>(psitab.p);
+                            for (int pass = 0; pass < 2; ++pass) {
+                                std::vector<cd> h(npsi);
+                                mdot_f32(pt, npsi, p, n, h.data(), ws, st);
+                                for (auto& x : h) x = -x;
+                                mcombine_f32(pt, npsi, h.data(), p, n, ws, st);
+                            }
+                            pn = std::sqrt(nrm2sq_f32(p, n, ws, st));
+                            if (pn < 0.5) continue;  // in the span of those held: the same Ritz value again
+                            scal_f32(1.0 / pn, p, n, st);
+                        }
+                        psi.p[npsi++] = p;
+                        QKG_CUDA(cudaMemcpyAsync(psitab.p, psi.p, sizeof(psi.p), cudaMemcpyHostToDevice, st));
+                        locked.push_back(theta);
                     }
                 }
             }
         };
         while (launched < nmax && stop_at < 0) {
             if (launched < kTimedSteps) {
-                enqueue_step(so_active, &timer);
+                enqueue_step(npsi, &timer);
                 out.t_spmv += timer.collect();  // waits for this SpMV only
                 ++out.n_spmv;
             } else {
-                cudaGraphExec_t& g = so_active ? g_so : g_plain;
-                if (!g) g = capture(so_active);
+                cudaGraphExec_t& g = graphs[npsi];
+                if (!g) g = capture(npsi);
                 QKG_CUDA(cudaGraphLaunch(g, st));
-                for (int q = 0; q < (so_active ? kernels_so : kernels_plain); ++q) count_launch();
+                for (int q = 0; q < kernels[npsi]; ++q) count_launch();
             }
-            if (so_active) ++out.n_selective;
+            if (npsi) ++out.n_selective;
             QKG_CUDA(cudaEventRecord(ev[launched % ev.size()], st));
             ++launched;
             while (checked < launched && stop_at < 0) {
@@ -460,13 +521,12 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     } catch (...) {
         cudaStreamSynchronize(st);
         for (auto& e : ev) cudaEventDestroy(e);
-        if (g_plain) cudaGraphExecDestroy(g_plain);
-        if (g_so) cudaGraphExecDestroy(g_so);
+        destroy_graphs();
         throw;
     }
     for (auto& e : ev) cudaEventDestroy(e);
-    if (g_plain) cudaGraphExecDestroy(g_plain);
-    if (g_so) cudaGraphExecDestroy(g_so);
+    destroy_graphs();
+    out.n_ritz_locked = npsi;
     out.t_loop = secs(t0, clk::now());
     if (stop_at < 0) stop_at = launched - 1;
     out.iters = stop_at + 1;

@@ -88,6 +88,12 @@ struct VecList {
         bufs.clear();
         host_ptrs.clear();
     }
+    void pop() {  // drop the newest vector
+        if (bufs.empty()) return;
+        if (pool) pool->put(std::move(bufs.back()));
+        bufs.pop_back();
+        host_ptrs.pop_back();
+    }
     void take(std::vector<DBuf>& nb) {
         clear();
         bufs = std::move(nb);
@@ -101,6 +107,45 @@ struct VecList {
 };
 
 size_t ws_cap(int k) { return std::max<size_t>(1 << 16, (size_t)1216 * (size_t)std::max(k, 1)); }
+
+// Appends the Ritz vector sum_i c_i V_i (normalised, Gram-Schmidt against the
+// Ritz vectors already held) to psi; false, with nothing appended, when it lies
+// in the span of those (the same Ritz value seen again).
+template <class T2>
+bool push_ritz(VecList<T2>& psi, const T2* const* V, int k, const std::vector<cd>& c, uint64_t n, Workspace& ws,
+               cudaStream_t st) {
+    constexpr bool F32 = sizeof(T2) == 8;
+    T2* p = psi.push();
+    QKG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T2), st));
+    auto nrm = [&](const T2* x) {
+        if constexpr (F32) return std::sqrt(nrm2sq_f32(x, n, ws, st));
+        else return std::sqrt(nrm2sq_f64(x, n, ws, st));
+    };
+    auto scal = [&](double a, T2* x) {
+        if constexpr (F32) scal_f32(a, x, n, st);
+        else scal_f64(a, x, n, st);
+    };
+    if constexpr (F32) mcombine_f32(V, k, c.data(), p, n, ws, st);
+    else mcombine_f64(V, k, c.data(), p, n, ws, st);
+    const double n0 = nrm(p);
+    if (!(n0 > 0.0)) { psi.pop(); return false; }
+    scal(1.0 / n0, p);
+    const int m = (int)psi.size() - 1;
+    if (m > 0) {
+        for (int pass = 0; pass < 2; ++pass) {  // twice is enough (Kahan's "twice is enough")
+            std::vector<cd> h(m);
+            if constexpr (F32) mdot_f32(psi.dev(), m, p, n, h.data(), ws, st);
+            else mdot_f64(psi.dev(), m, p, n, h.data(), ws, st);
+            for (auto& x : h) x = -x;
+            if constexpr (F32) mcombine_f32(psi.dev(), m, h.data(), p, n, ws, st);
+            else mcombine_f64(psi.dev(), m, h.data(), p, n, ws, st);
+        }
+        const double n1 = nrm(p);
+        if (n1 < 0.5) { psi.pop(); return false; }
+        scal(1.0 / n1, p);
+    }
+    return true;
+}
 
 void upload_ref_f64(Hamiltonian& H, const cd* host_ref, double2* d_int, DBuf& tmp) {
     const uint64_t n = H.dim();
@@ -241,6 +286,13 @@ double tridiag_ground(const double* a, const double* b, int n, std::vector<doubl
     if (n <= 0) { vec.clear(); return 0.0; }
     if (n == 1) { vec.assign(1, 1.0); return a[0]; }
     const double lam = tridiag_lowest(a, b, n);
+    if (!tridiag_vector(a, b, n, lam, vec)) return tridiag_ground_ql(a, b, n, vec);
+    return lam;
+}
+
+bool tridiag_vector(const double* a, const double* b, int n, double lam, std::vector<double>& vec) {
+    if (n <= 0) { vec.clear(); return true; }
+    if (n == 1) { vec.assign(1, 1.0); return true; }
     double tn = 0.0;
     for (int i = 0; i < n; ++i)
         tn = std::max(tn, std::abs(a[i]) + (i > 0 ? std::abs(b[i - 1]) : 0.0) + (i + 1 < n ? std::abs(b[i]) : 0.0));
@@ -288,7 +340,7 @@ double tridiag_ground(const double* a, const double* b, int n, std::vector<doubl
         double nr = 0.0;
         for (double v : x) nr += v * v;
         nr = std::sqrt(nr);
-        if (!(nr > 0.0) || !std::isfinite(nr)) return tridiag_ground_ql(a, b, n, vec);
+        if (!(nr > 0.0) || !std::isfinite(nr)) return false;
         for (double& v : x) v /= nr;
         if (it > 0) {
             double ov = 0.0;
@@ -302,7 +354,30 @@ double tridiag_ground(const double* a, const double* b, int n, std::vector<doubl
     for (int i = 1; i < n; ++i) if (std::abs(x[i]) > std::abs(x[im])) im = i;
     if (x[im] < 0) for (double& v : x) v = -v;
     vec = std::move(x);
-    return lam;
+    return true;
+}
+
+std::vector<double> ritz_to_lock(const double* a, const double* b, int k, double beta, double tol,
+                                 const std::vector<double>& locked, int max_locked) {
+    std::vector<double> out;
+    max_locked = std::max(1, std::min(max_locked, kMaxRitzLocked));
+    if (k < 4 || (int)locked.size() >= max_locked) return out;
+    std::vector<double> d, z;
+    tridiag_eig(a, b, k, d, {k - 1}, z);
+    std::vector<int> idx(k);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return d[x] < d[y]; });
+    double tn = 0.0;
+    for (double x : d) tn = std::max(tn, std::abs(x));
+    for (int r = 0; r < std::min(k, max_locked) && (int)(locked.size() + out.size()) < max_locked; ++r) {
+        const int i = idx[r];
+        if (beta * std::abs(z[i]) > tol * tn) continue;  // not converged
+        bool known = false;
+        for (double t : locked) known = known || std::abs(t - d[i]) <= tol * tn;
+        for (double t : out) known = known || std::abs(t - d[i]) <= tol * tn;
+        if (!known) out.push_back(d[i]);
+    }
+    return out;
 }
 
 // The same by the QL algorithm with every eigenvector row (O(n^3)): the
@@ -419,11 +494,12 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
     double e_old = 1e100;
     std::vector<cd> c;
     // o.selective: instead of the reference's full reorthogonalisation, the
-    // mixed form's scheme in FP64 (Parlett-Scott: once the lowest Ritz pair's
-    // residual estimate |beta_k s_k| <= sqrt(eps_64) ||T||, later vectors are
+    // mixed form's scheme in FP64 (Parlett-Scott: once one of the lowest Ritz
+    // pairs has converged, |beta_k s_k| <= sqrt(eps_64) ||T||, later vectors are
     // kept orthogonal to its Ritz vector) -- the control that separates the
     // mixed form's precision from its reorthogonalisation
     VecList<double2> psi(n);
+    std::vector<double> locked;  // Ritz values whose vectors are in psi
     const double so_tol = 1.5e-8;  // sqrt(eps_fp64)
     LaunchTimer timer(st);
     const auto t0 = clk::now();
@@ -468,27 +544,18 @@ LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
             if (std::abs(e - e_old) < o.tol) { out.converged = true; break; }
             e_old = e;
         }
-        if (o.selective && psi.size() == 0 && k >= 4) {
-            std::vector<double> d, z;
-            tridiag_eig(alphas.data(), betas.data(), k, d, {k - 1}, z);
-            int mi = 0;
-            for (int j = 1; j < k; ++j) if (d[j] < d[mi]) mi = j;
-            double tn = 0.0;
-            for (double x : d) tn = std::max(tn, std::abs(x));
-            if (beta * std::abs(z[mi]) <= so_tol * tn) {
-                std::vector<double> s;
-                tridiag_ground(alphas.data(), betas.data(), k, s);
-                std::vector<cd> cc(s.begin(), s.end());
-                double2* ps = psi.push();
-                QKG_CUDA(cudaMemsetAsync(ps, 0, n * sizeof(double2), st));
-                mcombine_f64(V.dev(), k, cc.data(), ps, n, ws, st);
-                const double pn = std::sqrt(nrm2sq_f64(ps, n, ws, st));
-                scal_f64(1.0 / pn, ps, n, st);
+        if (o.selective && k >= 4) {
+            for (double theta : ritz_to_lock(alphas.data(), betas.data(), k, beta, so_tol, locked, o.ritz_guard)) {
+                std::vector<double> sv;
+                if (!tridiag_vector(alphas.data(), betas.data(), k, theta, sv)) continue;
+                std::vector<cd> cc(sv.begin(), sv.end());
+                if (push_ritz(psi, V.dev(), k, cc, n, ws, st)) locked.push_back(theta);
             }
         }
     }
     QKG_CUDA(cudaStreamSynchronize(st));
     out.t_loop = secs(t0, clk::now());
+    out.n_ritz_locked = (int)psi.size();
     std::vector<double> s;
     out.energy = tridiag_ground(alphas.data(), betas.data(), (int)alphas.size(), s);
     out.energy_tridiag = out.energy;
@@ -527,6 +594,7 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
     Workspace ws(ws_cap(nmax + 2));
     VecList<float2> V(n);
     VecList<float2> psi(n);  // converged Ritz vectors used for selective reorthogonalisation
+    std::vector<double> locked;  // their Ritz values
     DBuf w(n * sizeof(float2)), tmp;
     float2* v = V.push();
     if (o.device_start) {
@@ -586,27 +654,19 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
             const double e = tridiag_lowest(alphas.data(), betas.data(), k);
             if (!o.fixed_steps && std::abs(e - e_old) < o.tol) { out.converged = true; break; }
             e_old = e;
-            // Selective reorthogonalisation: once the lowest Ritz pair has
-            // converged to FP32 level (|beta_k s_k| <= sqrt(eps) ||T||), keep
-            // later Lanczos vectors orthogonal to its Ritz vector.
-            if (psi.size() == 0 && k >= 4) {
-                std::vector<double> d, z;
-                tridiag_eig(alphas.data(), betas.data(), k, d, {k - 1}, z);
-                int mi = 0;
-                for (int j = 1; j < k; ++j) if (d[j] < d[mi]) mi = j;
-                double tn = 0.0;
-                for (int j = 0; j < k; ++j) tn = std::max(tn, std::abs(d[j]));
-                if (beta * std::abs(z[mi]) <= so_tol * tn) {
-                    std::vector<double> s;
-                    tridiag_ground(alphas.data(), betas.data(), k, s);
-                    float2* p = psi.push();
-                    QKG_CUDA(cudaMemsetAsync(p, 0, n * sizeof(float2), st));
-                    std::vector<cd> cc(s.begin(), s.end());
+            // Selective reorthogonalisation: once one of the lowest Ritz pairs
+            // has converged to FP32 level (|beta_k s_k| <= sqrt(eps) ||T||),
+            // keep later Lanczos vectors orthogonal to its Ritz vector.
+            if (k >= 4) {
+                for (double theta : ritz_to_lock(alphas.data(), betas.data(), k, beta, so_tol, locked, o.ritz_guard)) {
+                    std::vector<double> sv;
+                    if (!tridiag_vector(alphas.data(), betas.data(), k, theta, sv)) continue;
+                    std::vector<cd> cc(sv.begin(), sv.end());
                     V.sync_ptrs();
-                    mcombine_f32(V.dev(), k, cc.data(), p, n, ws, st);
-                    const double pn = std::sqrt(nrm2sq_f32(p, n, ws, st));
-                    scal_f32(1.0 / pn, p, n, st);
+                    if (!push_ritz(psi, V.dev(), k, cc, n, ws, st)) continue;
+                    locked.push_back(theta);
                     // the newest Lanczos vector is also made orthogonal to it
+                    const float2* p = psi[psi.size() - 1];
                     std::complex<double> cp = -dot_f32(p, vn, n, ws, st);
                     axpy_f32(cp, p, vn, n, st);
                     const double vnn = std::sqrt(nrm2sq_f32(vn, n, ws, st));
@@ -617,6 +677,7 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
     }
     QKG_CUDA(cudaStreamSynchronize(st));
     out.t_loop = secs(t0, clk::now());
+    out.n_ritz_locked = (int)psi.size();
     const auto t1 = clk::now();
     std::vector<double> s;
     out.energy_tridiag = tridiag_ground(alphas.data(), betas.data(), (int)alphas.size(), s);

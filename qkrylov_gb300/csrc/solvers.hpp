@@ -24,6 +24,16 @@ void tridiag_eig(const double* a, const double* b, int n, std::vector<double>& e
 // bisection and inverse iteration, O(n); _ql: the same by QL, O(n^3).
 double tridiag_ground(const double* a, const double* b, int n, std::vector<double>& vec);
 double tridiag_ground_ql(const double* a, const double* b, int n, std::vector<double>& vec);
+// Eigenvector for the eigenvalue lam by inverse iteration (false: breakdown).
+bool tridiag_vector(const double* a, const double* b, int n, double lam, std::vector<double>& vec);
+// Selective orthogonalisation (Parlett & Scott, Math. Comp. 33 (1979)): the
+// Ritz values among the max_locked (<= kMaxRitzLocked) lowest of T_k whose residual estimate
+// |beta_k s_{k,i}| <= tol ||T|| and that are not yet in `locked` (within
+// tol ||T||), ascending; later Lanczos vectors are kept orthogonal to their
+// Ritz vectors.
+constexpr int kMaxRitzLocked = 4;
+std::vector<double> ritz_to_lock(const double* a, const double* b, int k, double beta, double tol,
+                                 const std::vector<double>& locked, int max_locked = kMaxRitzLocked);
 // Hermitian m x m eigenproblem (cyclic complex Jacobi), ascending eigenvalues;
 // vecs[k][i] = component i of eigenvector k.
 void hermitian_eig(const std::vector<cd>& H, int m, std::vector<double>& evals, std::vector<std::vector<cd>>& vecs);
@@ -72,6 +82,8 @@ struct LanczosOpts {
     bool f32_stream = false;     // draw the start vector as the reference's FP32 engine does
     cd* evec_out = nullptr;      // with want_vec: the Ritz vector goes here (reference order) instead of LanczosOut::evec
     bool selective = false;      // FP64 form: selective instead of full reorthogonalisation (the mixed form's scheme)
+    int ritz_guard = 1;          // selective reorthogonalisation guards the converged Ritz vectors among the
+                                 // ritz_guard lowest (the wanted end: 1 for a ground state, <= kMaxRitzLocked)
 };
 struct LanczosOut {
     double energy = 0.0;       // reported energy (refined for the mixed form)
@@ -83,7 +95,8 @@ struct LanczosOut {
     std::vector<cd> evec;      // reference order
     double t_loop = 0.0;       // seconds in the Lanczos loop (device-synchronised)
     double t_refine = 0.0;
-    int n_selective = 0;       // steps that were re-orthogonalised against the Ritz vector
+    int n_selective = 0;       // steps that were re-orthogonalised against converged Ritz vectors
+    int n_ritz_locked = 0;     // converged Ritz vectors held at the end (selective reorthogonalisation)
     double t_spmv = 0.0;       // summed CUDA-event time of the loop's SpMV launches (seconds)
     int n_spmv = 0;
 };

@@ -166,7 +166,8 @@ def test_krylov_workspace_reused_across_runs(qk):
     f1 = qk.lanczos_fixed_steps(H, 40, seed=5, mixed=True)
     nbytes = H.workspace_bytes()
     stride = (H.dimension + 31) // 32 * 32
-    assert nbytes == (40 + 1 + 6) * stride * 8
+    # 41 Krylov vectors, 4 Ritz-vector slots, the FP32 Ritz vector, two FP64 vectors
+    assert nbytes == (40 + 1 + 4 + 1 + 4) * stride * 8
     f2 = qk.lanczos_fixed_steps(H, 40, seed=5, mixed=True)
     assert H.workspace_bytes() == nbytes
     assert (f1.energy, f1.energy_tridiag, f1.residual) == (f2.energy, f2.energy_tridiag, f2.residual)
@@ -236,3 +237,37 @@ def test_davidson_hubbard_L10_against_lanczos(qk, mixed):
     assert lam0 >= lz.energy - 1e-10 * abs(lz.energy)  # Rayleigh-Ritz: no Ritz value below E0
     assert lam0 - lz.energy <= res0 + 1e-10 * abs(lz.energy), (lam0, lz.energy, res0)
     assert np.all(np.diff(r.eigenvalues) >= -1e-12)
+
+
+def _random_chain(qk, L, seed):
+    """Open Heisenberg chain with random bonds and random longitudinal fields
+    (Sz conserved, no spatial symmetry: no degenerate levels)."""
+    rng = np.random.default_rng(seed)
+    ops = qk.OpSum()
+    for i in range(L - 1):
+        J = 0.5 + rng.random()
+        ops.add_term(J, "Sz", i, "Sz", i + 1)
+        ops.add_term(0.5 * J, "Sp", i, "Sm", i + 1)
+        ops.add_term(0.5 * J, "Sm", i, "Sp", i + 1)
+    for i in range(L):
+        ops.add_term(0.3 * (rng.random() - 0.5), "Sz", i)
+    return qk.MatrixFreeHamiltonian(qk.SpinHalfBasis(L, conserve_sz=True, sz=0), qk.SpinHalfSite(), ops)
+
+
+def test_selective_reorth_holds_several_ritz_vectors(qk):
+    # Parlett-Scott selective reorthogonalisation against every converged low
+    # Ritz vector (up to four): after many more steps than the ground state
+    # needs, the lowest Ritz values of the mixed form (FP32) and of FP64 with
+    # selective reorthogonalisation are those of FP64 with full
+    # reorthogonalisation and of the dense spectrum -- no ghost copies of a
+    # converged level among them
+    H = _random_chain(qk, 14, seed=11)  # dim 3432
+    exact = np.linalg.eigvalsh(H.to_sparse().toarray())[:5]
+    full, n0 = qk.lanczos_ritz_values(H, 300, 5, seed=3, mixed=False)
+    sel, n64 = qk.lanczos_ritz_values(H, 300, 5, seed=3, mixed=False, selective=True)
+    mix, n32 = qk.lanczos_ritz_values(H, 300, 5, seed=3, mixed=True)
+    assert n0 == 0
+    assert n64 >= 2 and n32 >= 2, (n64, n32)  # more than the ground state's Ritz vector is held
+    np.testing.assert_allclose(full, exact, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(sel, exact, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(mix, exact, rtol=0, atol=5e-5)  # FP32 vectors
