@@ -27,6 +27,7 @@
 #include "tile.hpp"
 
 #include <algorithm>
+#include <mutex>
 #include <atomic>
 #include <string>
 #include <cstring>
@@ -1527,10 +1528,22 @@ static void launch_fast(const FastParams<A>& p, size_t n_items, bool real, bool 
     QKG_LAUNCHED();
 }
 
-// Staged variants may need more than 48 KB of dynamic shared memory.
+// Staged variants may need more than 48 KB of dynamic shared memory.  The
+// attribute belongs to the kernel on the current device, not to a Hamiltonian:
+// it is raised once per device to the limit every staged launch stays under
+// (kStageLimit), so a Hamiltonian built later with a smaller slice cannot
+// shrink it below what an earlier one launches with.
 template <class T, class A>
 static void allow_stage_smem(size_t bytes) {
-    const int b = (int)bytes;
+    static std::mutex mu;
+    static uint64_t done = 0;  // devices already raised (bit per device id < 64)
+    if (bytes == 0) return;
+    int dev = 0;
+    QKG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (bit && (done & bit)) return;
+    const int b = (int)Hamiltonian::kStageLimit;
     QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     QKG_CUDA(cudaFuncSetAttribute(spmv_fast_kernel<T, A, false, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
@@ -1547,6 +1560,7 @@ static void allow_stage_smem(size_t bytes) {
     QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
     QKG_CUDA(cudaFuncSetAttribute(spmv_rows_kernel<T, A, true, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b));
+    done |= bit;
 }
 
 Hamiltonian::~Hamiltonian() {

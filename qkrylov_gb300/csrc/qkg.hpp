@@ -41,10 +41,13 @@ uint64_t launch_count();
 // Graph capture records launches without running them: the capturing code
 // takes them back (negative d) and adds the graph's kernels per replay.
 void add_launches(int64_t d);
-#define QKG_LAUNCHED()               \
-    do {                             \
-        ::qkg::count_launch();       \
-        QKG_CUDA(cudaGetLastError()); \
+#define QKG_LAUNCHED()                                                                                      \
+    do {                                                                                                   \
+        ::qkg::count_launch();                                                                             \
+        const cudaError_t le_ = cudaGetLastError();                                                        \
+        if (le_ != cudaSuccess)                                                                            \
+            throw ::qkg::Error(::qkg::CUDA_ERR, std::string("kernel launch at ") + __FILE__ + ":" +         \
+                                                    std::to_string(__LINE__) + ": " + cudaGetErrorString(le_)); \
     } while (0)
 // Device memory of the library goes through device_alloc/device_free: they
 // count the live allocations (qkrylov_debug_live_allocations) and let a test

@@ -101,6 +101,24 @@ def test_apply_and_diagonal(qk, name, mode):
         assert np.abs(y32 - g["y"]).max() <= RTOL32 * scale * 10
 
 
+@pytest.mark.parametrize("mode", [3, 5, 7, 10], ids=["fast-staged", "fast-rows4-staged", "tile1", "class"])
+def test_staged_variant_after_a_smaller_hamiltonian(qk, mode):
+    # a kernel's shared-memory limit is set per kernel and device, not per
+    # Hamiltonian: building a smaller model (a smaller staged slice) after a
+    # larger one must not make the larger one's staged launches fail
+    big = qk.MatrixFreeHamiltonian(*make_model(qk, *M.heisenberg(20, True, 0)))
+    big.select_kernel(mode=mode)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(big.dimension) + 1j * rng.standard_normal(big.dimension)
+    y0 = big.apply(x)
+    small = qk.MatrixFreeHamiltonian(*make_model(qk, *M.heisenberg(4, True, 0)))
+    small.apply(np.ones(small.dimension, dtype=np.complex128))
+    y1 = big.apply(x)
+    np.testing.assert_array_equal(y1, y0)
+    big.select_kernel(mode=1)  # the generic kernel as the reference
+    np.testing.assert_allclose(y1, big.apply(x), rtol=0, atol=RTOL64 * np.abs(y1).max())
+
+
 def test_fast_kernel_is_used_where_eligible(qk):
     for m in (M.heisenberg(16, True, 0), M.hubbard(8, True, 4, 4), (M.SPIN, 12, M.sector(), M.xyz_field_terms(12, True)),
               (M.FERMION, 14, M.sector(n=5), M.fermion_chain_terms(14, True))):
