@@ -78,6 +78,15 @@ def test_sector_semantics(qk):
     assert L.qkrylov_device_wait_timeouts(None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_hamiltonian_benchmark_apply(None, 1, 3, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_hamiltonian_tuning(None, 1, None, None) == qk.ERROR_INVALID_ARG
+    vals, n_out = np.zeros(4), ctypes.c_int()
+    dv = vals.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert L.qkrylov_lanczos_ritz_values(None, 10, 0, 1, 4, dv, ctypes.byref(n_out), None) == qk.ERROR_INVALID_ARG
+    out = np.zeros(2)
+    ptrs = (ctypes.c_void_p * 1)(16)
+    dp = out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert L.qkrylov_vector_mdot_device_f32(None, 1, ptrs, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_mdot_device_f32(ptrs, 0, ptrs, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_set_projection_kernel(2) == qk.ERROR_INVALID_ARG
 
 
 @pytest.mark.parametrize("name", golden_names())
