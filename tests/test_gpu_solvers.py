@@ -10,7 +10,7 @@ from oracle_ctypes import OHam, spectral
 
 pytestmark = pytest.mark.gpu
 
-E0_RTOL = 1e-10    # spec bar for E0 against the reference's FP64 Lanczos
+E0_RTOL = 1e-10    # the bar for E0 against the reference's FP64 Lanczos (relative)
 DYN_RTOL = 1e-8    # S(omega), FTLM Z/E/Cv
 
 
