@@ -289,6 +289,9 @@ int qkrylov_debug_device_wait_probe(int64_t limit_ns);
  * all work on the current GPU. */
 int qkrylov_set_device(int device_id);
 int qkrylov_device_synchronize(void);
+/* Visible CUDA devices (0 without a driver or device; the reference's
+ * Device::gpu_count, include/qkrylov/core/device.hpp:71-84). */
+int qkrylov_device_count(int* count);
 
 int qkrylov_davidson_lowest_complex_f64(qkrylov_hamiltonian_h h, int n_eig, int max_subspace, double tol,
                                         double* eigenvalues_out, double* eigenvectors_complex_out,

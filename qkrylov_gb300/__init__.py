@@ -11,6 +11,7 @@ meaning and result objects.  There is no CPU fallback: importing fails if the
 library has not been built (``python -m qkrylov_gb300.build``).
 """
 import ctypes as _c
+import enum as _enum
 import os as _os
 
 import numpy as _np
@@ -125,6 +126,7 @@ _SIGS = {
     "qkrylov_vector_dot_device_f32": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_vector_dot_device_f64_noalloc": (_i, [_vp, _vp, _u64, _dp, _vp]),
     "qkrylov_set_device": (_i, [_i]),
+    "qkrylov_device_count": (_i, [_ip]),
     "qkrylov_device_synchronize": (_i, []),
     "qkrylov_davidson_lowest_complex_f64": (_i, [_vp, _i, _i, _d, _dp, _dp, _c.POINTER(DavidsonResultC)]),
     "qkrylov_continued_fraction_coeffs_complex_f64": (_i, [_vp, _dp, _i, _dp, _dp, _dp, _ip, _ip]),
@@ -263,11 +265,15 @@ class Basis(_Handle):
         return out
 
 
+# The basis constructors take the reference facade's arguments
+# (bindings/python/qkrylov/basis.py:64-190).  ``dtype`` is accepted and unused:
+# bases are host tables here, and the arithmetic type is the Hamiltonian's.
 class SpinHalfBasis(Basis):
-    """Spin-1/2 chain; ``sz`` is the total Sz (the sector stores 2*Sz)."""
+    """Spin-1/2 chain; ``sz`` is the total Sz (the sector stores 2*Sz).  An
+    explicit ``sz`` conserves Sz; ``conserve_sz`` alone selects Sz = 0."""
     _create = "qkrylov_spinhalf_basis_create"
 
-    def __init__(self, N, conserve_sz=False, sz=None):
+    def __init__(self, N, conserve_sz=False, sz=None, dtype=None):
         if sz is not None or conserve_sz:
             super().__init__(N, Sector(sz2=int(round(2 * (sz or 0)))))
         else:
@@ -275,23 +281,29 @@ class SpinHalfBasis(Basis):
 
 
 class FermionBasis(Basis):
+    """Spinless fermions; a nonzero ``n`` (or ``conserve_n``) fixes the particle number."""
     _create = "qkrylov_fermion_basis_create"
 
-    def __init__(self, N, conserve_n=False, n=None):
-        if n is not None or conserve_n:
-            super().__init__(N, Sector(n=int(n or 0)))
+    def __init__(self, N, conserve_n=False, n=0, dtype=None):
+        if n or conserve_n:
+            super().__init__(N, Sector(n=int(n)))
         else:
             super().__init__(N)
 
 
 class HubbardBasis(Basis):
+    """Spin-1/2 electrons; a nonzero ``nup`` / ``ndn`` (or the conserve flag)
+    fixes that species' number, each independently."""
     _create = "qkrylov_hubbard_basis_create"
 
-    def __init__(self, N, nup=None, ndn=None):
-        super().__init__(N, Sector(nup=nup, ndn=ndn) if (nup is not None or ndn is not None) else None)
+    def __init__(self, N, conserve_nup=False, nup=0, conserve_ndn=False, ndn=0, dtype=None):
+        up = int(nup) if (nup or conserve_nup) else None
+        dn = int(ndn) if (ndn or conserve_ndn) else None
+        super().__init__(N, Sector(nup=up, ndn=dn) if (up is not None or dn is not None) else None)
 
 
 class TJBasis(HubbardBasis):
+    """t-J model: the Hubbard basis without doubly occupied sites."""
     _create = "qkrylov_tj_basis_create"
 
 
@@ -299,7 +311,7 @@ class Site(_Handle):
     _destroy = "qkrylov_site_destroy"
     _create = None
 
-    def __init__(self):
+    def __init__(self, dtype=None):  # dtype: the reference facade's argument, unused here
         self._h = getattr(lib(), self._create)()
 
 
@@ -324,15 +336,15 @@ class OpSum(_Handle):
     (include/qkrylov/operators/opsum.hpp:13-48)."""
     _destroy = "qkrylov_opsum_destroy"
 
-    def __init__(self):
+    def __init__(self, dtype=None):  # dtype: the reference facade's argument, unused here
         self._h = lib().qkrylov_opsum_create()
         self.terms = []
 
     def add_term(self, coeff, *ops_sites):
-        """add_term(coeff, "Sz", 0, "Sz", 1, ...)"""
+        """add_term(coeff, "Sz", 0, "Sz", 1, ...); an operator may also be an ``Op`` member."""
         if len(ops_sites) < 2 or len(ops_sites) % 2:
             raise ValueError("expected coeff followed by (op, site) pairs")
-        ops = [str(o) for o in ops_sites[0::2]]
+        ops = [o.value if isinstance(o, Op) else str(o) for o in ops_sites[0::2]]
         sites = [int(s) for s in ops_sites[1::2]]
         c = complex(coeff)
         arr = (_c.c_char_p * len(ops))(*[o.encode() for o in ops])
@@ -343,22 +355,51 @@ class OpSum(_Handle):
 
     def __iadd__(self, term):
         if isinstance(term, tuple):
+            if len(term) < 3 or len(term) % 2 == 0:
+                raise ValueError("Term must be a tuple of (coeff, op1, site1, ...)")
             return self.add_term(*term)
-        raise TypeError("OpSum += (coeff, op, site, ...)")
+        raise ValueError("Unsupported type for += on OpSum")
 
     def __len__(self):
         return len(self.terms)
+
+    @property
+    def size(self):
+        """Number of terms (the reference facade's OpSum.size)."""
+        return len(self.terms)
+
+    def clear(self):
+        _check(lib().qkrylov_opsum_clear(self._h))
+        self.terms = []
 
 
 class MatrixFreeHamiltonian(_Handle):
     """y = H x on the GPU (include/qkrylov/hamiltonian/matrix_free_hamiltonian.hpp:24-77)."""
     _destroy = "qkrylov_hamiltonian_destroy"
 
-    def __init__(self, basis, site, ops):
+    def __init__(self, basis, site, ops, device="cuda", dtype=_np.float64):
+        """``device`` and ``dtype`` are the reference facade's arguments
+        (bindings/python/qkrylov/hamiltonian.py:25-76).  Every Hamiltonian here
+        lives on a CUDA device: "cuda:N" / "gpu:N" select GPU N (the reference's
+        Device(id)), "cuda", "gpu" and "cpu" use the current one.  ``dtype``
+        np.float64 makes ``apply`` return complex128, np.float32 complex64
+        (computed in FP64 and rounded, as the float C ABI does)."""
         self.basis, self.site, self.ops = basis, site, ops
+        self.device = str(device)
+        self.dtype = _np.float32 if dtype in (_np.float32, "float32") else _np.float64
+        d = self.device.lower()
+        if ":" in d and (d.startswith("cuda") or d.startswith("gpu")):
+            set_device(int(d.split(":", 1)[1]))
+        elif d not in ("cuda", "gpu", "cpu"):
+            raise ValueError(f"unknown device {device!r}: expected 'cuda[:N]', 'gpu[:N]' or 'cpu'")
         self._h = lib().qkrylov_hamiltonian_create(basis._h, site._h, ops._h)
         if not self._h:
             raise ValueError((lib().qkrylov_last_error() or b"").decode() or "hamiltonian creation failed")
+
+    def to(self, device=None, dtype=None):
+        """A new Hamiltonian of the same basis, site and terms on ``device`` with ``dtype``."""
+        return MatrixFreeHamiltonian(self.basis, self.site, self.ops, device=self.device if device is None else device,
+                                     dtype=self.dtype if dtype is None else dtype)
 
     @property
     def dimension(self):
@@ -374,7 +415,7 @@ class MatrixFreeHamiltonian(_Handle):
         x = _cvec(x, self.dimension)
         y = _np.empty_like(x)
         _check(lib().qkrylov_hamiltonian_apply_complex_f64(self._h, _dptr(x.view(_np.float64)), _dptr(y.view(_np.float64))))
-        return y
+        return y.astype(_np.complex64) if self.dtype == _np.float32 else y
 
     def _apply_cuda(self, x):
         import torch
@@ -542,6 +583,50 @@ def set_projection_kernel(method):
 
 def set_device(device_id):
     _check(lib().qkrylov_set_device(int(device_id)))
+
+
+def gpu_count():
+    """Visible CUDA devices (the reference facade's gpu_count)."""
+    c = _c.c_int()
+    _check(lib().qkrylov_device_count(_c.byref(c)))
+    return int(c.value)
+
+
+def find_gpu():
+    """"cuda" when a GPU is visible, else None (the reference facade's find_gpu)."""
+    return "cuda" if gpu_count() > 0 else None
+
+
+class Device:
+    """The reference's Device (include/qkrylov/core/device.hpp:27-84):
+    Device(id) or Device("cuda:1") names a GPU; select() makes it current for
+    Hamiltonians created afterwards."""
+
+    def __init__(self, spec=0):
+        if isinstance(spec, str):
+            s = spec.lower()
+            self.id = int(s.split(":", 1)[1]) if ":" in s else 0
+        else:
+            self.id = int(spec)
+
+    def select(self):
+        set_device(self.id)
+        return self
+
+    @staticmethod
+    def is_gpu_build():
+        return True
+
+    @staticmethod
+    def backend_name():
+        return "cuda"
+
+    @staticmethod
+    def gpu_count():
+        return gpu_count()
+
+
+__version__ = "0.1.0"
 
 
 def synchronize():
@@ -750,6 +835,28 @@ def continued_fraction_block(H, phi0s, n_iter=100, mixed=True):
 
 
 # ------------------------------------------------------------------ expression sugar
+# The reference facade's operator algebra (bindings/python/qkrylov/operators.py):
+# Sz(0) * Sz(1) is a term, terms add into sums, numbers scale terms and sums,
+# and ``OpSum += expression`` appends the terms in order.
+class Op(str, _enum.Enum):
+    """Operator names (the reference facade's ``Op``)."""
+    Sz = "Sz"
+    Sp = "Sp"
+    Sm = "Sm"
+    Sx = "Sx"
+    Sy = "Sy"
+    CdagUp = "CdagUp"
+    CUp = "CUp"
+    CdagDn = "CdagDn"
+    CDn = "CDn"
+    Nup = "Nup"
+    Ndn = "Ndn"
+    Nupdn = "Nupdn"
+    Bdag = "Bdag"
+    B = "B"
+    N = "N"
+
+
 class LocalOp:
     def __init__(self, name, site):
         self.name, self.site = name, site
@@ -757,6 +864,8 @@ class LocalOp:
     def __mul__(self, other):
         if isinstance(other, LocalOp):
             return Term(1.0, [self, other])
+        if isinstance(other, Term):  # the operator stays on the left
+            return Term(other.coeff, [self] + other.ops)
         if isinstance(other, (int, float, complex)):
             return Term(complex(other), [self])
         return NotImplemented
@@ -780,10 +889,16 @@ class Term:
             return Term(self.coeff * complex(other), self.ops)
         return NotImplemented
 
-    __rmul__ = __mul__
+    def __rmul__(self, other):
+        if isinstance(other, (int, float, complex)):
+            return Term(self.coeff * complex(other), self.ops)
+        return NotImplemented
 
     def __add__(self, other):
         return Expr([self]) + other
+
+    def __sub__(self, other):
+        return Expr([self]) - other
 
 
 class Expr:
@@ -796,6 +911,20 @@ class Expr:
         if isinstance(other, Expr):
             return Expr(self.terms + other.terms)
         return NotImplemented
+
+    def __sub__(self, other):
+        if isinstance(other, Term):
+            return Expr(self.terms + [Term(-other.coeff, other.ops)])
+        if isinstance(other, Expr):
+            return Expr(self.terms + [Term(-t.coeff, t.ops) for t in other.terms])
+        return NotImplemented
+
+    def __mul__(self, other):
+        if isinstance(other, (int, float, complex)):
+            return Expr([t * other for t in self.terms])
+        return NotImplemented
+
+    __rmul__ = __mul__
 
 
 def _opsum_iadd(self, x):
@@ -814,7 +943,8 @@ def _opsum_iadd(self, x):
 _tuple_iadd = OpSum.__iadd__
 OpSum.__iadd__ = _opsum_iadd
 
-for _name in ("Sz", "Sp", "Sm", "Sx", "Sy", "CdagUp", "CUp", "CdagDn", "CDn", "Nup", "Ndn", "Nupdn", "N", "C", "Cdag", "Id"):
+for _name in ("Sz", "Sp", "Sm", "Sx", "Sy", "CdagUp", "CUp", "CdagDn", "CDn", "Nup", "Ndn", "Nupdn", "N", "C", "Cdag", "Id",
+              "B", "Bdag"):
     globals()[_name] = (lambda nm: (lambda i: LocalOp(nm, i)))(_name)
 
 

@@ -671,6 +671,16 @@ int qkrylov_debug_device_wait_probe(int64_t limit_ns) {
 int qkrylov_set_device(int id) {
     return guarded([&] { QKG_CUDA(cudaSetDevice(id)); });
 }
+int qkrylov_device_count(int* count) {
+    if (!count) return QKRYLOV_ERROR_INVALID_ARG;
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();  // no driver or no device: zero GPUs, not an error
+        c = 0;
+    }
+    *count = c;
+    return QKRYLOV_SUCCESS;
+}
 int qkrylov_device_synchronize(void) {
     return guarded([&] { QKG_CUDA(cudaDeviceSynchronize()); });
 }
