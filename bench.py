@@ -636,7 +636,7 @@ def davidson_hubbard(qk, cpu=True):
                     "evals": [float(x) for x in r64.eigenvalues],
                     "residuals": [float(x) for x in r64.residuals]},
            "E0_lanczos_fp64": {"value": e0, "steps": E0_CF_STEPS, "seconds": t_e0},
-           "form": "mixed: FP32 vectors and SpMV, compensated FP64-accurate projections, FP64-refined Ritz pairs"}
+           "form": "mixed: FP32 vectors and SpMV, run-summed FP32 projections (float-float across runs of 32), FP64-refined Ritz pairs"}
     for key, r in (("mixed", r32), ("fp64", r64)):
         d = abs(float(r.eigenvalues[0]) - e0)
         out[key]["lambda0_minus_E0"] = d

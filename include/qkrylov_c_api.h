@@ -260,14 +260,17 @@ int qkrylov_device_wait_timeouts(uint32_t* count);
  * method 0: compensated CUDA-core kernel (FP64-accurate sums, k nw <= 4088);
  * method 1: tensor cores (tcgen05, each product as hi*hi + hi*lo + lo*hi of
  * TF32 splits, FP32 sums of about a thousand products added in FP64;
- * k <= 128; a pointer off the 16-byte grid is QKRYLOV_ERROR_INVALID_ARG).
+ * k <= 128; a pointer off the 16-byte grid is QKRYLOV_ERROR_INVALID_ARG);
+ * method 2: CUDA cores, FP32 sums over runs of 32 elements folded into
+ * float-float sums (error about 6 u of sum |v||w|, u = 2^-24; k nw <= 4088).
  * Waits for `stream`.  Calls are serialised inside the library (one pointer
  * table and workspace per device, kept between calls). */
 int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
                                    int method, double* out, void* stream);
 /* Kernel the solvers' FP32 projections use (the mixed Davidson's projected
- * matrix and Gram-Schmidt passes): 0 the compensated CUDA-core kernel (the
- * default), 1 the tensor-core kernel where it applies.  Process-wide. */
+ * matrix and Gram-Schmidt passes): 0 the compensated CUDA-core kernel, 1 the
+ * tensor-core kernel where it applies, 2 the run-summed CUDA-core kernel
+ * (method 2 above; the default).  Process-wide. */
 int qkrylov_set_projection_kernel(int method);
 
 /* Test hooks (no counterpart in the reference).

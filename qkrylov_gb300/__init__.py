@@ -576,9 +576,11 @@ def device_wait_timeouts():
 
 
 def set_projection_kernel(method):
-    """Kernel of the solvers' FP32 projections: "cuda" (compensated CUDA-core,
-    FP64-accurate; the default) or "tensor" (tcgen05 tensor cores, 3xTF32)."""
-    _check(lib().qkrylov_set_projection_kernel({"cuda": 0, "tensor": 1}[method]))
+    """Kernel of the solvers' FP32 projections: "fast" (CUDA cores, FP32 sums
+    over runs of 32 elements folded into float-float sums; the default),
+    "cuda" (compensated CUDA-core, FP64-accurate) or "tensor" (tcgen05 tensor
+    cores, 3xTF32)."""
+    _check(lib().qkrylov_set_projection_kernel({"cuda": 0, "tensor": 1, "fast": 2}[method]))
 
 
 def set_device(device_id):
@@ -644,7 +646,8 @@ class DavidsonResult:
 
 def davidson_lowest_ex(H, n_eig=1, max_subspace=20, tol=1e-8, mixed=False, return_vectors=False, max_iter=100):
     """Davidson (davidson.cpp:86-227) in the FP64 form or the mixed form (FP32
-    vectors and SpMV, FP64-accurate projections, FP64-refined Ritz pairs).
+    vectors and SpMV, FP32 projections summed in runs and folded in float-float,
+    FP64-refined Ritz pairs).
     Returns a DavidsonResult with ``residuals`` and ``seconds`` set."""
     n = H.dimension
     k = min(int(n_eig), n)

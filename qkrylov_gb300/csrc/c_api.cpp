@@ -610,10 +610,10 @@ int qkrylov_device_wait_timeouts(uint32_t* count) {
 constexpr int kMdotMaxVectors = 4088;  // the CUDA-core kernel's limit on k * nw (k alone at nw = 1)
 int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
                                    int method, double* out, void* stream) {
-    if (!v_dev || !w_dev || !out || k < 1 || nw < 1 || nw > 4 || (method != 0 && method != 1))
+    if (!v_dev || !w_dev || !out || k < 1 || nw < 1 || nw > 4 || method < 0 || method > 2)
         return QKRYLOV_ERROR_INVALID_ARG;
     if (method == 1 && !qkg::mdot_tc_supported(k, nw)) return QKRYLOV_ERROR_INVALID_ARG;
-    if (method == 0 && (size_t)k * nw > 4088) return QKRYLOV_ERROR_INVALID_ARG;
+    if (method != 1 && (size_t)k * nw > 4088) return QKRYLOV_ERROR_INVALID_ARG;
     if (method == 1) {  // the tensor-core kernel copies 16-byte chunks
         for (int j = 0; j < k; ++j)
             if (reinterpret_cast<uintptr_t>(v_dev[j]) & 15u) return QKRYLOV_ERROR_INVALID_ARG;
@@ -644,6 +644,7 @@ int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* 
         std::vector<cd> r((size_t)k * nw);
         const auto* V = static_cast<const float2* const*>(sc.tab.p);
         if (method == 1) qkg::mdot_multi_f32_tc(V, k, w.data(), nw, n, r.data(), *sc.ws, s);
+        else if (method == 2) qkg::mdot_multi_f32_fast(V, k, w.data(), nw, n, r.data(), *sc.ws, s);
         else qkg::mdot_multi_f32_cuda(V, k, w.data(), nw, n, r.data(), *sc.ws, s);
         for (size_t i = 0; i < r.size(); ++i) {
             out[2 * i] = r[i].real();
@@ -653,7 +654,7 @@ int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* 
 }
 
 int qkrylov_set_projection_kernel(int method) {
-    if (method != 0 && method != 1) return QKRYLOV_ERROR_INVALID_ARG;
+    if (method < 0 || method > 2) return QKRYLOV_ERROR_INVALID_ARG;
     qkg::set_projection_mode(method);
     return QKRYLOV_SUCCESS;
 }

@@ -292,6 +292,9 @@ void mdot_multi_f32(const float2* const* V_dev, int k, float2* const* W, int nw,
 // The compensated CUDA-core kernel whatever the projection mode.
 void mdot_multi_f32_cuda(const float2* const* V_dev, int k, float2* const* W, int nw, uint64_t n,
                          std::complex<double>* out, Workspace& ws, cudaStream_t s);
+// the same with FP32 sums over runs of 32 elements (projection mode 2)
+void mdot_multi_f32_fast(const float2* const* V_dev, int k, float2* const* W, int nw, uint64_t n,
+                         std::complex<double>* out, Workspace& ws, cudaStream_t s);
 // The same on the tensor cores (tcgen05, 3xTF32 products, FP32 accumulation
 // read out into FP64 every thousand or so terms; mdot_tc.cu): k <= 128, nw <= 4.
 bool mdot_tc_supported(int k, int nw);

@@ -417,6 +417,117 @@ __global__ void __launch_bounds__(kThreads) mdot32_multi_kernel(const float2* co
             if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.x);
 }
 
+// The same projections with FP32 sums over short runs: every thread adds its
+// products with plain FP32 FMAs over kFastRun consecutive elements (16 pairs of
+// elements) and folds each run into a float-float sum (one TwoSum per run), so
+// the error is the FP32 rounding of sums of at most 2 kFastRun products, about
+// u sqrt(2 kFastRun) of their magnitude (u = 2^-24), instead of the compensated
+// kernel's FP64 level, at about a ninth of its FP32 operations.
+constexpr int kFastRun = 16;  // grid-stride iterations (two elements each) per run
+__device__ __forceinline__ void ff_add_f(FF& a, float t) {
+    const float s = a.hi + t;
+    const float z = s - a.hi;
+    a.lo += (a.hi - (s - z)) + (t - z);
+    a.hi = s;
+}
+template <int NW>
+__global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const float2* const* __restrict__ V, int k,
+                                                                     const float2* const* __restrict__ W, uint64_t n,
+                                                                     double2* part, int stride) {
+    const int j0 = blockIdx.y * KBM;
+    const int kk = min(KBM, k - j0);
+    FF re[KBM][NW], im[KBM][NW];
+    float tr[KBM][NW], ti[KBM][NW];
+    const float2* vp[KBM];
+    const float2* wp[NW];
+    bool al = true;
+#pragma unroll
+    for (int q = 0; q < KBM; ++q) {
+        vp[q] = V[j0 + (q < kk ? q : 0)];
+        al = al && (reinterpret_cast<uintptr_t>(vp[q]) & 15u) == 0;
+#pragma unroll
+        for (int o = 0; o < NW; ++o) {
+            re[q][o] = im[q][o] = FF{0.f, 0.f};
+            tr[q][o] = ti[q][o] = 0.f;
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < NW; ++o) {
+        wp[o] = W[o];
+        al = al && (reinterpret_cast<uintptr_t>(wp[o]) & 15u) == 0;
+    }
+    auto fold = [&]() {
+#pragma unroll
+        for (int q = 0; q < KBM; ++q)
+#pragma unroll
+            for (int o = 0; o < NW; ++o) {
+                ff_add_f(re[q][o], tr[q][o]);
+                ff_add_f(im[q][o], ti[q][o]);
+                tr[q][o] = ti[q][o] = 0.f;
+            }
+    };
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    uint64_t done = 0;
+    int run = 0;
+    if (al) {
+        const uint64_t n2 = n / 2;
+        for (uint64_t i = t0; i < n2; i += step) {
+            float4 b[NW];
+#pragma unroll
+            for (int o = 0; o < NW; ++o) b[o] = reinterpret_cast<const float4*>(wp[o])[i];
+#pragma unroll
+            for (int q = 0; q < KBM; ++q) {
+                if (q < kk) {
+                    const float4 a = reinterpret_cast<const float4*>(vp[q])[i];
+#pragma unroll
+                    for (int o = 0; o < NW; ++o) {
+                        float r = tr[q][o], m = ti[q][o];
+                        r = fmaf(a.x, b[o].x, r);
+                        r = fmaf(a.y, b[o].y, r);
+                        m = fmaf(a.x, b[o].y, m);
+                        m = fmaf(-a.y, b[o].x, m);
+                        r = fmaf(a.z, b[o].z, r);
+                        r = fmaf(a.w, b[o].w, r);
+                        m = fmaf(a.z, b[o].w, m);
+                        m = fmaf(-a.w, b[o].z, m);
+                        tr[q][o] = r;
+                        ti[q][o] = m;
+                    }
+                }
+            }
+            if (++run == kFastRun) {
+                fold();
+                run = 0;
+            }
+        }
+        done = 2 * n2;
+    }
+    for (uint64_t i = done + t0; i < n; i += step) {
+#pragma unroll
+        for (int q = 0; q < KBM; ++q)
+            if (q < kk) {
+                const float2 a = vp[q][i];
+#pragma unroll
+                for (int o = 0; o < NW; ++o) {
+                    const float2 b = wp[o][i];
+                    tr[q][o] = fmaf(a.y, b.y, fmaf(a.x, b.x, tr[q][o]));
+                    ti[q][o] = fmaf(-a.y, b.x, fmaf(a.x, b.y, ti[q][o]));
+                }
+            }
+        if (++run == kFastRun) {
+            fold();
+            run = 0;
+        }
+    }
+    fold();
+#pragma unroll
+    for (int q = 0; q < KBM; ++q)
+#pragma unroll
+        for (int o = 0; o < NW; ++o)
+            if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.x);
+}
+
 // w += sum_j c_j V_j ; coefficients (complex double) in global memory.
 template <class T2, class A>
 __global__ void mcomb_kernel(const T2* const* __restrict__ V, int k, const double2* __restrict__ c, T2* __restrict__ w,
@@ -633,7 +744,9 @@ void mdot_f32(const float2* const* V, int k, const float2* w, uint64_t n, std::c
     mdot_impl<float2, true>(V, k, w, n, out, ws, s);
 }
 namespace {
-std::atomic<int> g_projection_mode{0};
+// the run-summed kernel: at the mixed Davidson's accuracy (FP32 vectors) it
+// gives the compensated kernel's eigenvalues and residuals at about half the time
+std::atomic<int> g_projection_mode{2};
 }
 void set_projection_mode(int mode) { g_projection_mode.store(mode); }
 int projection_mode() { return g_projection_mode.load(); }
@@ -641,11 +754,39 @@ int projection_mode() { return g_projection_mode.load(); }
 void mdot_multi_f32(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,
                     Workspace& ws, cudaStream_t s) {
     if (k <= 0 || nw <= 0) return;
-    if (g_projection_mode.load() == 1 && mdot_tc_supported(k, nw)) {
+    const int mode = g_projection_mode.load();
+    if (mode == 1 && mdot_tc_supported(k, nw)) {
         mdot_multi_f32_tc(V, k, W, nw, n, out, ws, s);
         return;
     }
+    if (mode == 2) {
+        mdot_multi_f32_fast(V, k, W, nw, n, out, ws, s);
+        return;
+    }
     mdot_multi_f32_cuda(V, k, W, nw, n, out, ws, s);
+}
+
+void mdot_multi_f32_fast(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,
+                         Workspace& ws, cudaStream_t s) {
+    if (k <= 0 || nw <= 0) return;
+    QKG_REQUIRE(nw <= 4 && (size_t)k * nw <= 4088, "mdot_multi: at most 4 right-hand vectors and 4088 products");
+    float2** dw = reinterpret_cast<float2**>(ws.result.as<double2>() + 4096 - 8);
+    QKG_CUDA(cudaMemcpyAsync(dw, W, (size_t)nw * sizeof(float2*), cudaMemcpyHostToDevice, s));
+    int g = stream_grid(n);
+    g = (int)std::min<size_t>((size_t)g, ws.cap_partials / ((size_t)k * nw));
+    g = std::max(1, g);
+    const dim3 grid(g, (k + KBM - 1) / KBM);
+    double2* part = ws.partial.as<double2>();
+    switch (nw) {
+        case 1: mdot32_multi_fast_kernel<1><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        case 2: mdot32_multi_fast_kernel<2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        case 3: mdot32_multi_fast_kernel<3><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        default: mdot32_multi_fast_kernel<4><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+    }
+    QKG_LAUNCHED();
+    const double2* r = finish(ws, g, g, k * nw, s);
+    for (int j = 0; j < k; ++j)
+        for (int o = 0; o < nw; ++o) out[(size_t)o * k + j] = {r[(size_t)j * nw + o].x, r[(size_t)j * nw + o].y};
 }
 
 void mdot_multi_f32_cuda(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,

@@ -18,9 +18,9 @@ the seconds per iteration of the second run.  ``--peaks`` compiles and runs
 ``peaks.cu`` (FP64/FP32 FMA rates, L2 and DRAM read bandwidth, scattered
 8-byte reads from shared memory and L1) and prints its JSON line.  ``--mdot K``
 times the projections <V_j, W_o> of K FP32 vectors against ``--nw`` others of
-``--n`` complex elements (qkrylov_vector_mdot_device_f32) with both kernels,
-the compensated CUDA-core one and the tcgen05 one, and reports microseconds per
-call and the algorithmic bandwidth (every vector read once).  ``--lanczos N``
+``--n`` complex elements (qkrylov_vector_mdot_device_f32) with the three
+kernels (compensated CUDA-core, tcgen05, run-summed CUDA-core) and reports
+microseconds per call and the algorithmic bandwidth (every vector read once).  ``--lanczos N``
 runs N steps of the mixed Lanczos (qkrylov_lanczos_fixed_steps) on the
 Heisenberg chain, twice, and reports the mean time of its SpMV launches, each
 fused with the three-term recurrence (reads x and the previous Lanczos vector,
@@ -83,7 +83,7 @@ def main():
     p.add_argument("--mdot", type=int, default=0, help="vectors of a projection timing (0: none)")
     p.add_argument("--nw", type=int, default=4, help="right-hand vectors of the projection timing")
     p.add_argument("--n", type=int, default=50_000_000, help="vector length of the projection timing")
-    p.add_argument("--projection", choices=["cuda", "tensor"], default="cuda",
+    p.add_argument("--projection", choices=["cuda", "tensor", "fast"], default="fast",
                    help="kernel of the mixed Davidson's projections")
     a = p.parse_args()
     if a.peaks:
@@ -179,7 +179,7 @@ def mdot(a):
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     res = {"k": k, "nw": nw, "n": n, "bytes_per_call": (k + nw) * n * 8}
     vals = {}
-    for name, method in (("cuda", 0), ("tensor", 1)):
+    for name, method in (("cuda", 0), ("tensor", 1), ("fast", 2)):
         call = lambda: qk.lib().qkrylov_vector_mdot_device_f32(va, k, wa, nw, n, method, out, stream)
         for _ in range(3):
             assert call() == 0
@@ -191,7 +191,9 @@ def mdot(a):
         vals[name] = list(out)
         res[name + "_us"] = round(t * 1e6, 1)
         res[name + "_GBs"] = round(res["bytes_per_call"] / t / 1e9, 1)
-    res["max_rel_diff"] = max(abs(x - y) for x, y in zip(vals["cuda"], vals["tensor"])) / max(map(abs, vals["cuda"]))
+    big = max(map(abs, vals["cuda"]))
+    for name in ("tensor", "fast"):
+        res[name + "_max_rel_diff"] = max(abs(x - y) for x, y in zip(vals["cuda"], vals[name])) / big
     print(json.dumps(res), flush=True)
 
 

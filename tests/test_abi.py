@@ -86,7 +86,7 @@ def test_sector_semantics(qk):
     dp = out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     assert L.qkrylov_vector_mdot_device_f32(None, 1, ptrs, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_vector_mdot_device_f32(ptrs, 0, ptrs, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
-    assert L.qkrylov_set_projection_kernel(2) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_set_projection_kernel(3) == qk.ERROR_INVALID_ARG
 
 
 @pytest.mark.parametrize("name", golden_names())

@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 
 CUDA_RTOL = 1e-12  # compensated FP32 sums: FP64-level, relative to sum |v||w|
 TC_RTOL = 2e-6     # 3xTF32 products, FP32 partial sums of about a thousand products
+FAST_RTOL = 1e-6   # FP32 sums over runs of 32 products, folded into float-float sums
 
 
 def _cudart():
@@ -53,7 +54,7 @@ def test_projection_kernels_against_fp64(qk, n, k, nw):
     try:
         ref = np.conj(V.astype(np.complex128)) @ Wv.astype(np.complex128).T  # [k, nw]
         scale = np.abs(V).astype(np.float64) @ np.abs(Wv).astype(np.float64).T
-        for method, tol in ((0, CUDA_RTOL), (1, TC_RTOL)):
+        for method, tol in ((0, CUDA_RTOL), (1, TC_RTOL), (2, FAST_RTOL)):
             first = None
             for _ in range(2):  # a second call on the same data gives the same numbers
                 rc, got = _mdot(qk, dv, dw, n, method)
@@ -77,27 +78,29 @@ def test_projection_kernel_arguments(qk):
     # rejected before any device access
     assert L.qkrylov_vector_mdot_device_f32(va, 129, va, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG  # k > 128
     assert L.qkrylov_vector_mdot_device_f32(va, 1, va, 5, 8, 1, dp, None) == qk.ERROR_INVALID_ARG    # nw > 4
-    assert L.qkrylov_vector_mdot_device_f32(va, 1, va, 1, 8, 2, dp, None) == qk.ERROR_INVALID_ARG    # method
+    assert L.qkrylov_vector_mdot_device_f32(va, 1, va, 1, 8, 3, dp, None) == qk.ERROR_INVALID_ARG    # method
     v8 = (ctypes.c_void_p * 1)(24)  # off the 16-byte grid: the tensor-core kernel refuses it
     assert L.qkrylov_vector_mdot_device_f32(v8, 1, va, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_vector_mdot_device_f32(va, 1, v8, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_set_projection_kernel(7) == qk.ERROR_INVALID_ARG
 
 
+@pytest.mark.parametrize("kernel", ["tensor", "cuda", "fast"])
 @pytest.mark.parametrize("model", ["heis", "hub"])
-def test_mixed_davidson_with_tensor_projections(qk, model):
-    # the mixed Davidson with its projections on the tensor cores: eigenvalues
-    # agree with the FP64 form's as with the compensated kernel
+def test_mixed_davidson_with_each_projection_kernel(qk, model, kernel):
+    # the mixed Davidson with its projections on the tensor cores, the
+    # compensated kernel or the run-summed one (the default): eigenvalues agree
+    # with the FP64 form's
     if model == "heis":
         b, s, o = make_model(qk, M.SPIN, 14, M.sector(sz2=0), M.heisenberg_terms(14, True, Jz=0.9))
     else:
         b, s, o = make_model(qk, M.HUBBARD, 8, M.sector(nup=4, ndn=4), M.hubbard_terms(8, True))
     H = qk.MatrixFreeHamiltonian(b, s, o)
     r64 = qk.davidson_lowest_ex(H, n_eig=2, max_subspace=24, tol=1e-8, mixed=False)
-    qk.set_projection_kernel("tensor")
+    qk.set_projection_kernel(kernel)
     try:
         r32 = qk.davidson_lowest_ex(H, n_eig=2, max_subspace=24, tol=1e-5, mixed=True)
     finally:
-        qk.set_projection_kernel("cuda")
+        qk.set_projection_kernel("fast")  # the default
     assert np.all(np.asarray(r32.residuals) <= 3e-5), r32.residuals
     np.testing.assert_allclose(r32.eigenvalues, r64.eigenvalues, rtol=0, atol=1e-8)
