@@ -287,6 +287,18 @@ struct Mapped {
 
 bool lanczos_device_supported(const Hamiltonian& H) { return H.fast(); }
 
+// Device memory of a device-resident run of maxiter steps: maxiter + 1 Krylov
+// vectors, then kMaxPsi Ritz vectors psi (FP32), the Ritz vector (FP32), the
+// refined Ritz vector and its residual (FP64), each vector on a 256-byte
+// boundary.  The FP64 slots also stage a caller's start vector, the first two
+// psi slots the reference-order copy of the eigenvector.
+size_t lanczos_device_bytes(const Hamiltonian& H, int maxiter) {
+    const uint64_t n = H.dim();
+    const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(maxiter, 0), n);
+    const uint64_t stride = (n + 31) / 32 * 32;
+    return (size_t)(nmax + 1 + kMaxPsi + 5) * stride * sizeof(float2);
+}
+
 LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     LanczosOut out;
     const uint64_t n = H.dim();
@@ -299,11 +311,7 @@ LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o) {
     // vectors start on 256-byte boundaries (a warp's 32 consecutive rows then
     // cover whole 128-byte lines)
     const uint64_t stride = (n + 31) / 32 * 32;
-    // workspace: nmax + 1 Krylov vectors, then kMaxPsi Ritz vectors psi (FP32),
-    // the Ritz vector (FP32), the refined Ritz vector and its residual (FP64);
-    // the FP64 slots also stage a caller's start vector, the first two psi
-    // slots the reference-order copy of the eigenvector
-    const size_t need = (size_t)(nmax + 1 + kMaxPsi + 5) * stride * sizeof(float2);
+    const size_t need = lanczos_device_bytes(H, o.maxiter);
     if (H.workspace_bytes() < need) {
         H.release_workspace();
         size_t fr = 0, tot = 0;

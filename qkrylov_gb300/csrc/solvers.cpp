@@ -463,12 +463,24 @@ void ref_uniform_complex(uint32_t seed, uint64_t n, cd* out, bool f32) {
 }
 
 // ============================================================ Lanczos (FP64)
+// A Krylov workspace an earlier mixed run left on H is freed when a run that
+// allocates its own vectors (bytes of them) would not fit beside it.
+void release_workspace_if_short(Hamiltonian& H, size_t bytes) {
+    if (!H.workspace_bytes()) return;
+    size_t fr = 0, tot = 0;
+    QKG_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (bytes + (1ull << 30) < fr) return;
+    const auto ws_lock = H.workspace_lock();
+    H.release_workspace();
+}
+
 LanczosOut lanczos_f64(Hamiltonian& H, const LanczosOpts& o) {
     LanczosOut out;
     const uint64_t n = H.dim();
     if (n == 0) return out;
     cudaStream_t st = H.stream();
     const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);
+    release_workspace_if_short(H, (size_t)(nmax + 3) * n * sizeof(double2));
     Workspace ws(ws_cap(nmax + 2));
     VecList<double2> V(n);
     DBuf w(n * sizeof(double2)), tmp;
@@ -586,8 +598,13 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o) {
     if (lanczos_device_supported(H)) {
         size_t fr = 0, tot = 0;
         QKG_CUDA(cudaMemGetInfo(&fr, &tot));
-        const uint64_t k = std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n) + 1;
-        if (k * n * sizeof(float2) + (1ull << 30) < fr) return lanczos_mixed_device(H, o);
+        // the Krylov workspace an earlier run left on the Hamiltonian is reused
+        // (or freed first) by the device-resident run: it counts as available
+        const size_t held = H.workspace_bytes();
+        if (lanczos_device_bytes(H, o.maxiter) + (1ull << 30) < fr + held) return lanczos_mixed_device(H, o);
+        // the host-driven run allocates its own vectors: give it that memory back
+        const auto ws_lock = H.workspace_lock();
+        H.release_workspace();
     }
     cudaStream_t st = H.stream();
     const int nmax = (int)std::min<uint64_t>((uint64_t)std::max(o.maxiter, 0), n);

@@ -124,6 +124,8 @@ LanczosOut lanczos_mixed(Hamiltonian& H, const LanczosOpts& o);
 // The same mixed form with a device-resident recurrence (one CUDA graph per
 // step); needs the fast SpMV kernel and room for maxiter + 1 FP32 vectors.
 bool lanczos_device_supported(const Hamiltonian& H);
+// device memory a device-resident mixed run of maxiter steps holds
+size_t lanczos_device_bytes(const Hamiltonian& H, int maxiter);
 LanczosOut lanczos_mixed_device(Hamiltonian& H, const LanczosOpts& o);
 
 // ---- continued fraction (src/solvers/dynamics.cpp:13-89) --------------------------
