@@ -1,4 +1,5 @@
-"""Eigenvector / tridiagonal files (CPU: bases are host objects)."""
+"""Eigenvector / tridiagonal files: the formats on the host, and a GPU ground
+state and continued fraction written, read back and reused."""
 import numpy as np
 import pytest
 
@@ -44,3 +45,40 @@ def test_tridiagonals_roundtrip(qk, tmp_path):
         assert n0 == n1
     with pytest.raises(ValueError):
         qk.io.load_eigenvector(p)
+
+
+@pytest.mark.gpu
+def test_ground_state_checkpoint_and_restart(qk, tmp_path):
+    # a GPU ground state written to a file and read back is still an
+    # eigenvector of H, and a Lanczos run restarted from it converges at once
+    basis, site, ops = M.make_model(qk, *M.heisenberg(16, True, 0))
+    H = qk.MatrixFreeHamiltonian(basis, site, ops)
+    r = qk.lanczos_ground_state(H, maxiter=300, tol=1e-13)
+    p = str(tmp_path / "gs.npz")
+    qk.io.save_eigenvector(p, r.eigenvector[None, :], [r.energy], basis, extra={"iterations": r.iterations})
+    v, e, meta = qk.io.load_eigenvector(p, basis)
+    psi = v[0]
+    hpsi = H.apply(psi)
+    assert np.linalg.norm(hpsi - e[0] * psi) < 1e-5
+    assert abs(np.vdot(psi, hpsi).real - r.energy) < 1e-10 * abs(r.energy)
+    again = qk.lanczos_ground_state(H, maxiter=300, tol=1e-13, v0=psi)
+    assert abs(again.energy - r.energy) < 1e-10 * abs(r.energy)
+    assert again.iterations < r.iterations
+
+
+@pytest.mark.gpu
+def test_continued_fraction_file_gives_the_same_spectrum(qk, tmp_path):
+    # S(omega) evaluated from tridiagonals written and read back equals the
+    # value from the GPU run itself
+    basis, site, ops = M.make_model(qk, *M.heisenberg(12, True, 0))
+    H = qk.MatrixFreeHamiltonian(basis, site, ops)
+    gs = qk.lanczos_ground_state(H, maxiter=200, tol=1e-12)
+    phi = gs.eigenvector * np.linspace(0.5, 1.5, H.dimension)
+    cf = qk.continued_fraction_coeffs(H, phi, n_iter=80)
+    p = str(tmp_path / "cf.npz")
+    qk.io.save_tridiagonals(p, [(cf.alphas, cf.betas, cf.norm_phi0)], basis)
+    (a, bb, nrm), = qk.io.load_tridiagonals(p, basis)[0]
+    back = qk.DynamicsResult(a, bb, nrm)
+    om = np.linspace(0.0, 4.0, 41)
+    np.testing.assert_array_equal(qk.evaluate_spectral_function(back, om, gs.energy, 0.1),
+                                  qk.evaluate_spectral_function(cf, om, gs.energy, 0.1))
