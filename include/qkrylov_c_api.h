@@ -267,6 +267,16 @@ int qkrylov_device_wait_timeouts(uint32_t* count);
  * table and workspace per device, kept between calls). */
 int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
                                    int method, double* out, void* stream);
+/* Combinations of device vectors, the update half of a block Gram-Schmidt
+ * (no counterpart in the reference, whose Davidson subtracts one axpy per pair,
+ * src/solvers/davidson.cpp:213-223): W_o = (accumulate ? W_o : 0) +
+ * sum_j C_oj V_j for o < nw <= 8, j < k, k nw <= 1024, with
+ * C_oj = coeffs[2 (o k + j)] + i coeffs[2 (o k + j) + 1] (rounded to FP32) and
+ * FP32 sums in ascending j.  One pass over the V_j for all outputs.  Returns
+ * when the kernel has been queued on `stream` and the host arrays may be
+ * reused. */
+int qkrylov_vector_mcombine_device_f32(const void* const* v_dev, int k, const double* coeffs, void* const* w_dev,
+                                       int nw, uint64_t n, int accumulate, void* stream);
 /* Kernel the solvers' FP32 projections use (the mixed Davidson's projected
  * matrix and Gram-Schmidt passes): 0 the compensated CUDA-core kernel, 1 the
  * tensor-core kernel where it applies, 2 the run-summed CUDA-core kernel

@@ -118,6 +118,8 @@ _SIGS = {
     "qkrylov_debug_inject_alloc_failure": (_i, [_c.c_int64]),
     "qkrylov_vector_mdot_device_f32": (_i, [_c.POINTER(_c.c_void_p), _i, _c.POINTER(_c.c_void_p), _i, _c.c_uint64, _i,
                                             _dp, _vp]),
+    "qkrylov_vector_mcombine_device_f32": (_i, [_c.POINTER(_c.c_void_p), _i, _dp, _c.POINTER(_c.c_void_p), _i,
+                                                _c.c_uint64, _i, _vp]),
     "qkrylov_set_projection_kernel": (_i, [_i]),
     "qkrylov_lanczos_ritz_values": (_i, [_vp, _i, _c.c_uint64, _i, _i, _dp, _ip, _ip]),
     "qkrylov_debug_live_allocations": (_c.c_int64, []),

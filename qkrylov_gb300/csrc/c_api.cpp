@@ -608,6 +608,29 @@ int qkrylov_device_wait_timeouts(uint32_t* count) {
     return rc;
 }
 constexpr int kMdotMaxVectors = 4088;  // the CUDA-core kernel's limit on k * nw (k alone at nw = 1)
+namespace {
+// One pointer table and workspace per device for the projection and
+// combination entry points, kept between calls (no allocation per call);
+// calls are serialised.
+struct VectorScratch {
+    qkg::DBuf tab;
+    std::unique_ptr<qkg::Workspace> ws;
+};
+std::mutex g_vector_scratch_mu;
+std::unique_lock<std::mutex> vector_scratch_lock() { return std::unique_lock<std::mutex>(g_vector_scratch_mu); }
+VectorScratch& vector_scratch() {  // caller holds vector_scratch_lock()
+    static std::map<int, VectorScratch> scratch;
+    int dev = 0;
+    QKG_CUDA(cudaGetDevice(&dev));
+    VectorScratch& sc = scratch[dev];
+    if (!sc.ws) {
+        sc.tab.alloc((size_t)kMdotMaxVectors * sizeof(void*));
+        sc.ws = std::make_unique<qkg::Workspace>(1 << 16);
+    }
+    return sc;
+}
+}  // namespace
+
 int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
                                    int method, double* out, void* stream) {
     if (!v_dev || !w_dev || !out || k < 1 || nw < 1 || nw > 4 || method < 0 || method > 2)
@@ -622,22 +645,8 @@ int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* 
     }
     return guarded([&] {
         cudaStream_t s = static_cast<cudaStream_t>(stream);
-        // one pointer table and workspace per device, kept between calls (no
-        // allocation per call); calls are serialised
-        struct Scratch {
-            qkg::DBuf tab;
-            std::unique_ptr<qkg::Workspace> ws;
-        };
-        static std::mutex mu;
-        static std::map<int, Scratch> scratch;
-        int dev = 0;
-        QKG_CUDA(cudaGetDevice(&dev));
-        std::lock_guard<std::mutex> lk(mu);
-        Scratch& sc = scratch[dev];
-        if (!sc.ws) {
-            sc.tab.alloc((size_t)kMdotMaxVectors * sizeof(void*));
-            sc.ws = std::make_unique<qkg::Workspace>(1 << 16);
-        }
+        auto lk = vector_scratch_lock();
+        VectorScratch& sc = vector_scratch();
         QKG_CUDA(cudaMemcpyAsync(sc.tab.p, v_dev, (size_t)k * sizeof(void*), cudaMemcpyHostToDevice, s));
         std::vector<float2*> w(nw);
         for (int o = 0; o < nw; ++o) w[o] = const_cast<float2*>(static_cast<const float2*>(w_dev[o]));
@@ -650,6 +659,25 @@ int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* 
             out[2 * i] = r[i].real();
             out[2 * i + 1] = r[i].imag();
         }
+    });
+}
+
+int qkrylov_vector_mcombine_device_f32(const void* const* v_dev, int k, const double* coeffs, void* const* w_dev,
+                                       int nw, uint64_t n, int accumulate, void* stream) {
+    if (!v_dev || !w_dev || (!coeffs && k > 0) || k < 0 || nw < 1 || nw > 8 || (size_t)k * nw > 1024)
+        return QKRYLOV_ERROR_INVALID_ARG;
+    return guarded([&] {
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        auto lk = vector_scratch_lock();
+        VectorScratch& sc = vector_scratch();
+        if (k > 0)
+            QKG_CUDA(cudaMemcpyAsync(sc.tab.p, v_dev, (size_t)k * sizeof(void*), cudaMemcpyHostToDevice, s));
+        std::vector<float2*> w(nw);
+        for (int o = 0; o < nw; ++o) w[o] = static_cast<float2*>(w_dev[o]);
+        std::vector<cd> c((size_t)k * nw);
+        for (size_t i = 0; i < c.size(); ++i) c[i] = {coeffs[2 * i], coeffs[2 * i + 1]};
+        qkg::mcombine_multi_f32(static_cast<const float2* const*>(sc.tab.p), k, c.data(), w.data(), nw, n,
+                                accumulate != 0, *sc.ws, s);
     });
 }
 

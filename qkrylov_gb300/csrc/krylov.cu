@@ -248,11 +248,15 @@ __global__ void lupd32_kernel(float2* __restrict__ w, const float2* __restrict__
 }
 
 // Projections <V_j, w> for a group of up to KB vectors per block column.
+// Grid of all projection kernels: x = column (group of vectors), y = row chunk
+// (grid-stride over the elements).  x varies fastest in launch order, so the
+// columns of one row chunk run side by side on the same elements and w (or W)
+// comes from DRAM once and from L2 for the other columns.
 constexpr int KB = 8;
 template <class T2, bool F32>
 __global__ void mdot_kernel(const T2* const* __restrict__ V, int k, const T2* __restrict__ w, uint64_t n, double2* part,
                             int stride) {
-    const int j0 = blockIdx.y * KB;
+    const int j0 = blockIdx.x * KB;
     const int kk = min(KB, k - j0);
     double re[KB], im[KB];
     FF fre[KB], fim[KB];
@@ -261,7 +265,7 @@ __global__ void mdot_kernel(const T2* const* __restrict__ V, int k, const T2* __
     const T2* vp[KB];
 #pragma unroll
     for (int q = 0; q < KB; ++q) vp[q] = (q < kk) ? V[j0 + q] : nullptr;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t i = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.y * blockDim.x) {
         const T2 b = w[i];
 #pragma unroll
         for (int q = 0; q < KB; ++q) {
@@ -286,7 +290,7 @@ __global__ void mdot_kernel(const T2* const* __restrict__ V, int k, const T2* __
         if (q < kk) {
             const double2 v = F32 ? make_double2(ff_value(fre[q]), ff_value(fim[q])) : make_double2(re[q], im[q]);
             const double2 s = block_sum(v);
-            if (threadIdx.x == 0) part[(size_t)(j0 + q) * stride + blockIdx.x] = s;
+            if (threadIdx.x == 0) part[(size_t)(j0 + q) * stride + blockIdx.y] = s;
         }
     }
 }
@@ -304,7 +308,7 @@ __device__ __forceinline__ void ff_cmac(FF& re, FF& im, float ax, float ay, floa
 __global__ void __launch_bounds__(kThreads) mdot32_kernel(const float2* const* __restrict__ V, int k,
                                                           const float2* __restrict__ w, uint64_t n, double2* part,
                                                           int stride) {
-    const int j0 = blockIdx.y * KB32;
+    const int j0 = blockIdx.x * KB32;
     const int kk = min(KB32, k - j0);
     FF re[KB32], im[KB32];
     const float2* vp[KB32];
@@ -315,8 +319,8 @@ __global__ void __launch_bounds__(kThreads) mdot32_kernel(const float2* const* _
         vp[q] = V[j0 + (q < kk ? q : 0)];
         al = al && (reinterpret_cast<uintptr_t>(vp[q]) & 15u) == 0;
     }
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t step = (uint64_t)gridDim.y * blockDim.x;
+    const uint64_t t0 = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x;
     uint64_t done = 0;
     if (al) {
         const uint64_t n2 = n / 2;
@@ -345,7 +349,7 @@ __global__ void __launch_bounds__(kThreads) mdot32_kernel(const float2* const* _
     }
 #pragma unroll
     for (int q = 0; q < KB32; ++q) {
-        if (q < kk) block_sum_cff(re[q], im[q], part + (size_t)(j0 + q) * stride + blockIdx.x);
+        if (q < kk) block_sum_cff(re[q], im[q], part + (size_t)(j0 + q) * stride + blockIdx.y);
     }
 }
 
@@ -357,7 +361,7 @@ template <int NW>
 __global__ void __launch_bounds__(kThreads) mdot32_multi_kernel(const float2* const* __restrict__ V, int k,
                                                                 const float2* const* __restrict__ W, uint64_t n,
                                                                 double2* part, int stride) {
-    const int j0 = blockIdx.y * KBM;
+    const int j0 = blockIdx.x * KBM;
     const int kk = min(KBM, k - j0);
     FF re[KBM][NW], im[KBM][NW];
     const float2* vp[KBM];
@@ -375,8 +379,8 @@ __global__ void __launch_bounds__(kThreads) mdot32_multi_kernel(const float2* co
         wp[o] = W[o];
         al = al && (reinterpret_cast<uintptr_t>(wp[o]) & 15u) == 0;
     }
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t step = (uint64_t)gridDim.y * blockDim.x;
+    const uint64_t t0 = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x;
     uint64_t done = 0;
     if (al) {
         const uint64_t n2 = n / 2;
@@ -414,7 +418,7 @@ __global__ void __launch_bounds__(kThreads) mdot32_multi_kernel(const float2* co
     for (int q = 0; q < KBM; ++q)
 #pragma unroll
         for (int o = 0; o < NW; ++o)
-            if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.x);
+            if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.y);
 }
 
 // The same projections with FP32 sums over short runs: every thread adds its
@@ -422,7 +426,8 @@ __global__ void __launch_bounds__(kThreads) mdot32_multi_kernel(const float2* co
 // elements) and folds each run into a float-float sum (one TwoSum per run), so
 // the error is the FP32 rounding of sums of at most 2 kFastRun products, about
 // u sqrt(2 kFastRun) of their magnitude (u = 2^-24), instead of the compensated
-// kernel's FP64 level, at about a ninth of its FP32 operations.
+// kernel's FP64 level, at about a ninth of its FP32 operations.  KC basis
+// vectors per column (CTA).
 constexpr int kFastRun = 16;  // grid-stride iterations (two elements each) per run
 __device__ __forceinline__ void ff_add_f(FF& a, float t) {
     const float s = a.hi + t;
@@ -430,19 +435,19 @@ __device__ __forceinline__ void ff_add_f(FF& a, float t) {
     a.lo += (a.hi - (s - z)) + (t - z);
     a.hi = s;
 }
-template <int NW>
-__global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const float2* const* __restrict__ V, int k,
+template <int NW, int KC>
+__global__ void __launch_bounds__(kThreads, KC == 4 ? 2 : 3) mdot32_multi_fast_kernel(const float2* const* __restrict__ V, int k,
                                                                      const float2* const* __restrict__ W, uint64_t n,
                                                                      double2* part, int stride) {
-    const int j0 = blockIdx.y * KBM;
-    const int kk = min(KBM, k - j0);
-    FF re[KBM][NW], im[KBM][NW];
-    float tr[KBM][NW], ti[KBM][NW];
-    const float2* vp[KBM];
+    const int j0 = blockIdx.x * KC;
+    const int kk = min(KC, k - j0);
+    FF re[KC][NW], im[KC][NW];
+    float tr[KC][NW], ti[KC][NW];
+    const float2* vp[KC];
     const float2* wp[NW];
     bool al = true;
 #pragma unroll
-    for (int q = 0; q < KBM; ++q) {
+    for (int q = 0; q < KC; ++q) {
         vp[q] = V[j0 + (q < kk ? q : 0)];
         al = al && (reinterpret_cast<uintptr_t>(vp[q]) & 15u) == 0;
 #pragma unroll
@@ -458,7 +463,7 @@ __global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const fl
     }
     auto fold = [&]() {
 #pragma unroll
-        for (int q = 0; q < KBM; ++q)
+        for (int q = 0; q < KC; ++q)
 #pragma unroll
             for (int o = 0; o < NW; ++o) {
                 ff_add_f(re[q][o], tr[q][o]);
@@ -466,8 +471,8 @@ __global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const fl
                 tr[q][o] = ti[q][o] = 0.f;
             }
     };
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t step = (uint64_t)gridDim.y * blockDim.x;
+    const uint64_t t0 = blockIdx.y * (uint64_t)blockDim.x + threadIdx.x;
     uint64_t done = 0;
     int run = 0;
     if (al) {
@@ -477,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const fl
 #pragma unroll
             for (int o = 0; o < NW; ++o) b[o] = reinterpret_cast<const float4*>(wp[o])[i];
 #pragma unroll
-            for (int q = 0; q < KBM; ++q) {
+            for (int q = 0; q < KC; ++q) {
                 if (q < kk) {
                     const float4 a = reinterpret_cast<const float4*>(vp[q])[i];
 #pragma unroll
@@ -505,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const fl
     }
     for (uint64_t i = done + t0; i < n; i += step) {
 #pragma unroll
-        for (int q = 0; q < KBM; ++q)
+        for (int q = 0; q < KC; ++q)
             if (q < kk) {
                 const float2 a = vp[q][i];
 #pragma unroll
@@ -522,10 +527,10 @@ __global__ void __launch_bounds__(kThreads, 2) mdot32_multi_fast_kernel(const fl
     }
     fold();
 #pragma unroll
-    for (int q = 0; q < KBM; ++q)
+    for (int q = 0; q < KC; ++q)
 #pragma unroll
         for (int o = 0; o < NW; ++o)
-            if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.x);
+            if (q < kk) block_sum_cff(re[q][o], im[q][o], part + ((size_t)(j0 + q) * NW + o) * stride + blockIdx.y);
 }
 
 // w += sum_j c_j V_j ; coefficients (complex double) in global memory.
@@ -724,11 +729,11 @@ static void mdot_impl(const T2* const* V, int k, const T2* w, uint64_t n, std::c
     g = (int)std::min<size_t>((size_t)g, ws.cap_partials / (size_t)k);
     g = std::max(1, g);
     if (F32) {
-        dim3 grid(g, (k + KB32 - 1) / KB32);
+        dim3 grid((k + KB32 - 1) / KB32, g);
         mdot32_kernel<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float2* const*>(V), k,
                                                 reinterpret_cast<const float2*>(w), n, ws.partial.as<double2>(), g);
     } else {
-        dim3 grid(g, (k + KB - 1) / KB);
+        dim3 grid((k + KB - 1) / KB, g);
         mdot_kernel<T2, F32><<<grid, kThreads, 0, s>>>(V, k, w, n, ws.partial.as<double2>(), g);
     }
     QKG_LAUNCHED();
@@ -775,13 +780,26 @@ void mdot_multi_f32_fast(const float2* const* V, int k, float2* const* W, int nw
     int g = stream_grid(n);
     g = (int)std::min<size_t>((size_t)g, ws.cap_partials / ((size_t)k * nw));
     g = std::max(1, g);
-    const dim3 grid(g, (k + KBM - 1) / KBM);
+    // columns of 2 basis vectors for 3-4 right-hand vectors (80 registers, 3
+    // CTAs per SM; W's re-reads come from L2), of 4 for 1-2 (at k = 32, n = 11.8 M:
+    // nw = 4 1.00 against 1.42 ms, nw = 1 0.18 against 0.16 ms)
     double2* part = ws.partial.as<double2>();
-    switch (nw) {
-        case 1: mdot32_multi_fast_kernel<1><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-        case 2: mdot32_multi_fast_kernel<2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-        case 3: mdot32_multi_fast_kernel<3><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-        default: mdot32_multi_fast_kernel<4><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+    if (nw >= 3) {
+        const dim3 grid((k + 1) / 2, g);
+        switch (nw) {
+            case 1: mdot32_multi_fast_kernel<1, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+            case 2: mdot32_multi_fast_kernel<2, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+            case 3: mdot32_multi_fast_kernel<3, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+            default: mdot32_multi_fast_kernel<4, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        }
+    } else {
+        const dim3 grid((k + KBM - 1) / KBM, g);
+        switch (nw) {
+            case 1: mdot32_multi_fast_kernel<1, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+            case 2: mdot32_multi_fast_kernel<2, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+            case 3: mdot32_multi_fast_kernel<3, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+            default: mdot32_multi_fast_kernel<4, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
+        }
     }
     QKG_LAUNCHED();
     const double2* r = finish(ws, g, g, k * nw, s);
@@ -799,7 +817,7 @@ void mdot_multi_f32_cuda(const float2* const* V, int k, float2* const* W, int nw
     int g = stream_grid(n);
     g = (int)std::min<size_t>((size_t)g, ws.cap_partials / ((size_t)k * nw));
     g = std::max(1, g);
-    const dim3 grid(g, (k + KBM - 1) / KBM);
+    const dim3 grid((k + KBM - 1) / KBM, g);
     double2* part = ws.partial.as<double2>();
     switch (nw) {
         case 1: mdot32_multi_kernel<1><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;

@@ -7,6 +7,7 @@ profiles are taken with).
 
     python -m qkrylov_gb300.timing --peaks
     python -m qkrylov_gb300.timing --mdot 32 --nw 4 --n 50000000 --reps 20
+    python -m qkrylov_gb300.timing --mcomb 32 --nw 4 --n 50000000 --reps 20
     python -m qkrylov_gb300.timing --L 28 --lanczos 8 [--mode 4]
 
 The second form runs the batched Lanczos on every Sz sector of the chain (or
@@ -20,7 +21,9 @@ the seconds per iteration of the second run.  ``--peaks`` compiles and runs
 times the projections <V_j, W_o> of K FP32 vectors against ``--nw`` others of
 ``--n`` complex elements (qkrylov_vector_mdot_device_f32) with the three
 kernels (compensated CUDA-core, tcgen05, run-summed CUDA-core) and reports
-microseconds per call and the algorithmic bandwidth (every vector read once).  ``--lanczos N``
+microseconds per call and the algorithmic bandwidth (every vector read once).  ``--mcomb K``
+times the combinations W_o = sum_j C_oj V_j of K FP32 vectors into ``--nw`` outputs
+(qkrylov_vector_mcombine_device_f32, CUDA events, ``--reps`` calls).  ``--lanczos N``
 runs N steps of the mixed Lanczos (qkrylov_lanczos_fixed_steps) on the
 Heisenberg chain, twice, and reports the mean time of its SpMV launches, each
 fused with the three-term recurrence (reads x and the previous Lanczos vector,
@@ -81,7 +84,8 @@ def main():
     p.add_argument("--peaks", action="store_true", help="FMA / L2 / DRAM / gather throughput probes")
     p.add_argument("--lanczos", type=int, default=0, help="mixed Lanczos steps (0: none)")
     p.add_argument("--mdot", type=int, default=0, help="vectors of a projection timing (0: none)")
-    p.add_argument("--nw", type=int, default=4, help="right-hand vectors of the projection timing")
+    p.add_argument("--mcomb", type=int, default=0, help="vectors of a combination timing (0: none)")
+    p.add_argument("--nw", type=int, default=4, help="right-hand vectors (outputs) of the projection (combination) timing")
     p.add_argument("--n", type=int, default=50_000_000, help="vector length of the projection timing")
     p.add_argument("--projection", choices=["cuda", "tensor", "fast"], default="fast",
                    help="kernel of the mixed Davidson's projections")
@@ -94,6 +98,8 @@ def main():
         return davidson(a)
     if a.mdot:
         return mdot(a)
+    if a.mcomb:
+        return mcomb(a)
     if a.lanczos:
         return lanczos(a)
     build = heisenberg_chain if a.model == "heisenberg" else hubbard_chain
@@ -195,6 +201,34 @@ def mdot(a):
     for name in ("tensor", "fast"):
         res[name + "_max_rel_diff"] = max(abs(x - y) for x, y in zip(vals["cuda"], vals[name])) / big
     print(json.dumps(res), flush=True)
+
+
+def mcomb(a):
+    """W_o = sum_j C_oj V_j (qkrylov_vector_mcombine_device_f32), CUDA-event timed."""
+    import ctypes
+    import torch
+    k, nw, n = a.mcomb, a.nw, a.n
+    g = torch.Generator(device="cuda").manual_seed(1)
+    V = [torch.randn(n, dtype=torch.complex64, device="cuda", generator=g) for _ in range(k)]
+    W = [torch.empty(n, dtype=torch.complex64, device="cuda") for _ in range(nw)]
+    va = (ctypes.c_void_p * k)(*[v.data_ptr() for v in V])
+    wa = (ctypes.c_void_p * nw)(*[w.data_ptr() for w in W])
+    c = (ctypes.c_double * (2 * k * nw))(*[((i * 7) % 13 - 6) / 13.0 for i in range(2 * k * nw)])
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    call = lambda: qk.lib().qkrylov_vector_mcombine_device_f32(va, k, c, wa, nw, n, 0, stream)
+    for _ in range(3):
+        assert call() == 0
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.reps):
+        assert call() == 0
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / a.reps
+    nbytes = (k + nw) * n * 8
+    print(json.dumps({"k": k, "nw": nw, "n": n, "bytes_per_call": nbytes, "us": round(t * 1e6, 1),
+                      "GBs": round(nbytes / t / 1e9, 1)}), flush=True)
 
 
 if __name__ == "__main__":

@@ -70,6 +70,38 @@ def test_projection_kernels_against_fp64(qk, n, k, nw):
             cudart.cudaFree(p)
 
 
+@pytest.mark.parametrize("n,k,nw,acc", [(1_000_003, 32, 4, 0), (4097, 1, 1, 1), (5, 3, 2, 1), (70_001, 7, 8, 0),
+                                        (300_000, 128, 8, 1), (33, 0, 3, 1), (33, 0, 2, 0)])
+def test_combination_against_fp64(qk, n, k, nw, acc):
+    # W_o = (acc ? W_o : 0) + sum_j C_oj V_j, the update half of the block
+    # Gram-Schmidt; FP32 sums in ascending j, held to their rounding bound
+    cudart = _cudart()
+    rng = np.random.default_rng(n + k + nw)
+    V = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))).astype(np.complex64)
+    W0 = (rng.standard_normal((nw, n)) + 1j * rng.standard_normal((nw, n))).astype(np.complex64)
+    C = rng.standard_normal((nw, k)) + 1j * rng.standard_normal((nw, k))
+    dv = [_dev(cudart, V[j]) for j in range(k)]
+    dw = [_dev(cudart, W0[o]) for o in range(nw)]
+    try:
+        va = (ctypes.c_void_p * max(1, k))(*[p.value for p in dv])
+        wa = (ctypes.c_void_p * nw)(*[p.value for p in dw])
+        cf = np.ascontiguousarray(C).view(np.float64)
+        rc = qk.lib().qkrylov_vector_mcombine_device_f32(va, k, cf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                         wa, nw, n, acc, None)
+        assert rc == 0, qk.lib().qkrylov_last_error()
+        C32 = C.astype(np.complex64).astype(np.complex128)
+        ref = C32 @ V.astype(np.complex128) + (W0.astype(np.complex128) if acc else 0)
+        scale = np.abs(C32) @ np.abs(V).astype(np.float64) + (np.abs(W0) if acc else 0) + 1e-30
+        got = np.empty((nw, n), dtype=np.complex64)
+        for o in range(nw):
+            assert cudart.cudaMemcpy(got[o].ctypes.data_as(ctypes.c_void_p), dw[o], got[o].nbytes, 2) == 0
+        err = np.abs(got - ref) / scale
+        assert err.max() <= 4 * (k + 2) * 2.0 ** -24, err.max()
+    finally:
+        for p in dv + dw:
+            cudart.cudaFree(p)
+
+
 def test_projection_kernel_arguments(qk):
     out = np.zeros(2)
     va = (ctypes.c_void_p * 1)(16)
@@ -83,6 +115,10 @@ def test_projection_kernel_arguments(qk):
     assert L.qkrylov_vector_mdot_device_f32(v8, 1, va, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_vector_mdot_device_f32(va, 1, v8, 1, 8, 1, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_set_projection_kernel(7) == qk.ERROR_INVALID_ARG
+    cp = np.zeros(2 * 1025).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert L.qkrylov_vector_mcombine_device_f32(va, 1, cp, va, 9, 8, 0, None) == qk.ERROR_INVALID_ARG   # nw > 8
+    assert L.qkrylov_vector_mcombine_device_f32(va, 129, cp, va, 8, 8, 0, None) == qk.ERROR_INVALID_ARG  # k nw > 1024
+    assert L.qkrylov_vector_mcombine_device_f32(va, 1, None, va, 1, 8, 0, None) == qk.ERROR_INVALID_ARG  # no coefficients
 
 
 @pytest.mark.parametrize("kernel", ["tensor", "cuda", "fast"])
