@@ -64,15 +64,17 @@ __device__ __forceinline__ void vload(const typename V2<T>::t* p, typename V2<T>
     }
 }
 
+// y is written once per step and next read by the update pass: stored
+// evict-first (cache-streaming), so the gathered x keeps more of L2
 template <class T, int VPL>
 __device__ __forceinline__ void vstore(typename V2<T>::t* p, const typename V2<T>::t (&v)[VPL]) {
     if constexpr (sizeof(T) == 4 && VPL % 2 == 0) {
 #pragma unroll
         for (int j = 0; j < VPL; j += 2)
-            reinterpret_cast<float4*>(p)[j / 2] = make_float4(v[j].x, v[j].y, v[j + 1].x, v[j + 1].y);
+            __stcs(reinterpret_cast<float4*>(p) + j / 2, make_float4(v[j].x, v[j].y, v[j + 1].x, v[j + 1].y));
     } else {
 #pragma unroll
-        for (int j = 0; j < VPL; ++j) p[j] = v[j];
+        for (int j = 0; j < VPL; ++j) __stcs(p + j, v[j]);
     }
 }
 

@@ -716,7 +716,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         dc[q] = p.diag_mode == DIAG_U8 ? (uint32_t)__ldg(static_cast<const uint8_t*>(p.dcode) + row)
                                        : (uint32_t)__ldg(static_cast<const uint16_t*>(p.dcode) + row);
         xd[q] = (STAGE && staged_ok) ? xst[rl] : x[row];
-        if (vprev) pv[q] = vprev[row];
+        // v_{k-1} and y are touched once per step: loaded and stored evict-first
+        // (cache-streaming), so the gathered x keeps more of L2
+        if (vprev) pv[q] = __ldcs(vprev + row);
     }
 #pragma unroll
     for (int q = 0; q < RT; ++q) {
@@ -737,7 +739,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? (WIDE ? QKG_ROWS_MINB
         T2 out;
         out.x = (T)o_r;
         out.y = (T)o_i;
-        y[(uint32_t)it.row0 + pass + tbase + q * 32u] = out;
+        __stcs(y + ((uint32_t)it.row0 + pass + tbase + q * 32u), out);
         if (p.apart) {
             ffma_acc(dot_hi, dot_lo, (A)xd[q].x, (A)out.x);
             ffma_acc(dot_hi, dot_lo, (A)xd[q].y, (A)out.y);
