@@ -780,26 +780,25 @@ void mdot_multi_f32_fast(const float2* const* V, int k, float2* const* W, int nw
     int g = stream_grid(n);
     g = (int)std::min<size_t>((size_t)g, ws.cap_partials / ((size_t)k * nw));
     g = std::max(1, g);
-    // columns of 2 basis vectors for 3-4 right-hand vectors (80 registers, 3
+    // Columns of 2 basis vectors for 3-4 right-hand vectors (80 registers, 3
     // CTAs per SM; W's re-reads come from L2), of 4 for 1-2 (at k = 32, n = 11.8 M:
-    // nw = 4 1.00 against 1.42 ms, nw = 1 0.18 against 0.16 ms)
+    // nw = 4 1.00 against 1.42 ms, nw = 1 0.18 against 0.16 ms).  Row chunks for
+    // two resident waves of CTAs in all, rounded down (a last, nearly empty wave
+    // of whole chunks would double the time): at k = 32, nw = 4, n = 11.8 M
+    // 0.93 ms, against 1.02 ms for 512 chunks and 1.71 ms for one wave rounded up.
     double2* part = ws.partial.as<double2>();
-    if (nw >= 3) {
-        const dim3 grid((k + 1) / 2, g);
-        switch (nw) {
-            case 1: mdot32_multi_fast_kernel<1, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-            case 2: mdot32_multi_fast_kernel<2, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-            case 3: mdot32_multi_fast_kernel<3, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-            default: mdot32_multi_fast_kernel<4, 2><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-        }
-    } else {
-        const dim3 grid((k + KBM - 1) / KBM, g);
-        switch (nw) {
-            case 1: mdot32_multi_fast_kernel<1, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-            case 2: mdot32_multi_fast_kernel<2, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-            case 3: mdot32_multi_fast_kernel<3, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-            default: mdot32_multi_fast_kernel<4, KBM><<<grid, kThreads, 0, s>>>(V, k, dw, n, part, g); break;
-        }
+    auto launch = [&](auto kern, int kc) {
+        const int ncol = (k + kc - 1) / kc;
+        int per_sm = 1;
+        QKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
+        g = std::min(g, std::max(1, 152 * std::max(1, per_sm) * 2 / ncol));
+        kern<<<dim3(ncol, g), kThreads, 0, s>>>(V, k, dw, n, part, g);
+    };
+    switch (nw) {
+        case 1: launch(mdot32_multi_fast_kernel<1, KBM>, KBM); break;
+        case 2: launch(mdot32_multi_fast_kernel<2, KBM>, KBM); break;
+        case 3: launch(mdot32_multi_fast_kernel<3, 2>, 2); break;
+        default: launch(mdot32_multi_fast_kernel<4, 2>, 2); break;
     }
     QKG_LAUNCHED();
     const double2* r = finish(ws, g, g, k * nw, s);
