@@ -163,7 +163,10 @@ int qkrylov_hamiltonian_diagonal_f64(qkrylov_hamiltonian_h h, double* diag_out /
 
 /* Same, but x and y are device pointers (reference order) and the work is
  * queued on `stream` (a cudaStream_t, NULL = legacy default stream); the call
- * returns without synchronising.  The _f32 form runs the FP32 kernel. */
+ * returns without synchronising.  The _f32 form runs the FP32 kernel.  Device
+ * pointers of this section must sit on the grid of whole complex elements
+ * (16 bytes for complex FP64, 8 for complex FP32), else
+ * QKRYLOV_ERROR_INVALID_ARG before any launch. */
 int qkrylov_hamiltonian_apply_device_f64(qkrylov_hamiltonian_h h, const void* d_x, void* d_y, void* stream);
 int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* d_x, void* d_y, void* stream);
 
@@ -263,6 +266,8 @@ int qkrylov_device_wait_timeouts(uint32_t* count);
  * k <= 128; a pointer off the 16-byte grid is QKRYLOV_ERROR_INVALID_ARG);
  * method 2: CUDA cores, FP32 sums over runs of 32 elements folded into
  * float-float sums (error about 6 u of sum |v||w|, u = 2^-24; k nw <= 4088).
+ * Every pointer must be 8-byte aligned (16-byte for method 1); others are
+ * QKRYLOV_ERROR_INVALID_ARG.
  * Waits for `stream`.  Calls are serialised inside the library (one pointer
  * table and workspace per device, kept between calls). */
 int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* const* w_dev, int nw, uint64_t n,
@@ -272,7 +277,8 @@ int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* 
  * src/solvers/davidson.cpp:213-223): W_o = (accumulate ? W_o : 0) +
  * sum_j C_oj V_j for o < nw <= 8, j < k, k nw <= 1024, with
  * C_oj = coeffs[2 (o k + j)] + i coeffs[2 (o k + j) + 1] (rounded to FP32) and
- * FP32 sums in ascending j.  One pass over the V_j for all outputs.  Returns
+ * FP32 sums in ascending j.  One pass over the V_j for all outputs; every
+ * pointer 8-byte aligned (else QKRYLOV_ERROR_INVALID_ARG).  Returns
  * when the kernel has been queued on `stream` and the host arrays may be
  * reused. */
 int qkrylov_vector_mcombine_device_f32(const void* const* v_dev, int k, const double* coeffs, void* const* w_dev,

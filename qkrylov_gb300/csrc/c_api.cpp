@@ -337,8 +337,12 @@ int qkrylov_hamiltonian_diagonal_f64(qkrylov_hamiltonian_h h, double* d) {
     });
 }
 
+// Device vectors are read and written as whole complex elements (8-byte float2,
+// 16-byte double2): a pointer off that grid is refused before any launch.
+static bool on_grid(const void* p, uintptr_t bytes) { return (reinterpret_cast<uintptr_t>(p) & (bytes - 1)) == 0; }
+
 int qkrylov_hamiltonian_apply_device_f64(qkrylov_hamiltonian_h h, const void* dx, void* dy, void* stream) {
-    if (!h || !h->ptr || !dx || !dy) return QKRYLOV_ERROR_INVALID_ARG;
+    if (!h || !h->ptr || !dx || !dy || !on_grid(dx, 16) || !on_grid(dy, 16)) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         auto& H = *h->ptr;
         set_device(h);
@@ -358,7 +362,7 @@ int qkrylov_hamiltonian_apply_device_f64(qkrylov_hamiltonian_h h, const void* dx
     });
 }
 int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* dx, void* dy, void* stream) {
-    if (!h || !h->ptr || !dx || !dy) return QKRYLOV_ERROR_INVALID_ARG;
+    if (!h || !h->ptr || !dx || !dy || !on_grid(dx, 8) || !on_grid(dy, 8)) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         auto& H = *h->ptr;
         set_device(h);
@@ -379,7 +383,7 @@ int qkrylov_hamiltonian_apply_device_f32(qkrylov_hamiltonian_h h, const void* dx
 }
 
 int qkrylov_vector_dot_device_f64(const void* dx, const void* dy, uint64_t n, double* result, void* stream) {
-    if (!result || (n && (!dx || !dy))) return QKRYLOV_ERROR_INVALID_ARG;
+    if (!result || (n && (!dx || !dy || !on_grid(dx, 16) || !on_grid(dy, 16)))) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         result[0] = result[1] = 0.0;
         if (!n) return;
@@ -390,7 +394,7 @@ int qkrylov_vector_dot_device_f64(const void* dx, const void* dy, uint64_t n, do
     });
 }
 int qkrylov_vector_dot_device_f32(const void* dx, const void* dy, uint64_t n, double* result, void* stream) {
-    if (!result || (n && (!dx || !dy))) return QKRYLOV_ERROR_INVALID_ARG;
+    if (!result || (n && (!dx || !dy || !on_grid(dx, 8) || !on_grid(dy, 8)))) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         result[0] = result[1] = 0.0;
         if (!n) return;
@@ -637,12 +641,13 @@ int qkrylov_vector_mdot_device_f32(const void* const* v_dev, int k, const void* 
         return QKRYLOV_ERROR_INVALID_ARG;
     if (method == 1 && !qkg::mdot_tc_supported(k, nw)) return QKRYLOV_ERROR_INVALID_ARG;
     if (method != 1 && (size_t)k * nw > 4088) return QKRYLOV_ERROR_INVALID_ARG;
-    if (method == 1) {  // the tensor-core kernel copies 16-byte chunks
-        for (int j = 0; j < k; ++j)
-            if (reinterpret_cast<uintptr_t>(v_dev[j]) & 15u) return QKRYLOV_ERROR_INVALID_ARG;
-        for (int o = 0; o < nw; ++o)
-            if (reinterpret_cast<uintptr_t>(w_dev[o]) & 15u) return QKRYLOV_ERROR_INVALID_ARG;
-    }
+    // complex FP32 elements are loaded as 8-byte pairs (16-byte chunks by the
+    // tensor-core kernel): a pointer off that grid is refused before any launch
+    const uintptr_t grid = method == 1 ? 16u : 8u;
+    for (int j = 0; j < k; ++j)
+        if (!on_grid(v_dev[j], grid)) return QKRYLOV_ERROR_INVALID_ARG;
+    for (int o = 0; o < nw; ++o)
+        if (!on_grid(w_dev[o], grid)) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         auto lk = vector_scratch_lock();
@@ -666,6 +671,10 @@ int qkrylov_vector_mcombine_device_f32(const void* const* v_dev, int k, const do
                                        int nw, uint64_t n, int accumulate, void* stream) {
     if (!v_dev || !w_dev || (!coeffs && k > 0) || k < 0 || nw < 1 || nw > 8 || (size_t)k * nw > 1024)
         return QKRYLOV_ERROR_INVALID_ARG;
+    for (int j = 0; j < k; ++j)
+        if (!on_grid(v_dev[j], 8)) return QKRYLOV_ERROR_INVALID_ARG;
+    for (int o = 0; o < nw; ++o)
+        if (!on_grid(w_dev[o], 8)) return QKRYLOV_ERROR_INVALID_ARG;
     return guarded([&] {
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         auto lk = vector_scratch_lock();

@@ -122,6 +122,8 @@ double2* na_scratch_on_current_device() {
 extern "C" int qkrylov_vector_dot_device_f64_noalloc(const void* d_x, const void* d_y, uint64_t n, double* result,
                                                      void* stream) {
     if (!result || (n && (!d_x || !d_y))) return QKRYLOV_ERROR_INVALID_ARG;
+    // whole complex FP64 elements (16-byte loads): a pointer off that grid is refused
+    if (n && ((reinterpret_cast<uintptr_t>(d_x) | reinterpret_cast<uintptr_t>(d_y)) & 15u)) return QKRYLOV_ERROR_INVALID_ARG;
     if (n > kNoAllocMaxElements) {
         qkg::set_last_error("qkrylov_vector_dot_device_f64_noalloc: n = " + std::to_string(n) +
                             " exceeds the fixed scratch limit of " + std::to_string(kNoAllocMaxElements) +

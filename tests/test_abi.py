@@ -86,6 +86,13 @@ def test_sector_semantics(qk):
     dp = out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     assert L.qkrylov_vector_mdot_device_f32(None, 1, ptrs, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_vector_mdot_device_f32(ptrs, 0, ptrs, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
+    # device pointers off the grid of whole complex elements: refused before any launch
+    res = (ctypes.c_double * 2)()
+    assert L.qkrylov_vector_dot_device_f64(ctypes.c_void_p(24), ctypes.c_void_p(32), 4, res, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_dot_device_f32(ctypes.c_void_p(16), ctypes.c_void_p(20), 4, res, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_dot_device_f64_noalloc(ctypes.c_void_p(8), ctypes.c_void_p(16), 4, res, None) == qk.ERROR_INVALID_ARG
+    bad = (ctypes.c_void_p * 1)(12)
+    assert L.qkrylov_vector_mcombine_device_f32(bad, 1, dp, ptrs, 1, 8, 0, None) == qk.ERROR_INVALID_ARG
     assert L.qkrylov_set_projection_kernel(3) == qk.ERROR_INVALID_ARG
 
 

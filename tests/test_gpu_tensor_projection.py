@@ -119,6 +119,11 @@ def test_projection_kernel_arguments(qk):
     assert L.qkrylov_vector_mcombine_device_f32(va, 1, cp, va, 9, 8, 0, None) == qk.ERROR_INVALID_ARG   # nw > 8
     assert L.qkrylov_vector_mcombine_device_f32(va, 129, cp, va, 8, 8, 0, None) == qk.ERROR_INVALID_ARG  # k nw > 1024
     assert L.qkrylov_vector_mcombine_device_f32(va, 1, None, va, 1, 8, 0, None) == qk.ERROR_INVALID_ARG  # no coefficients
+    v4 = (ctypes.c_void_p * 1)(20)  # off the 8-byte grid of complex FP32 elements
+    assert L.qkrylov_vector_mdot_device_f32(v4, 1, va, 1, 8, 2, dp, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_mdot_device_f32(va, 1, v4, 1, 8, 0, dp, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_mcombine_device_f32(v4, 1, cp, va, 1, 8, 0, None) == qk.ERROR_INVALID_ARG
+    assert L.qkrylov_vector_mcombine_device_f32(va, 1, cp, v4, 1, 8, 0, None) == qk.ERROR_INVALID_ARG
 
 
 @pytest.mark.parametrize("kernel", ["tensor", "cuda", "fast"])
