@@ -771,6 +771,20 @@ void mdot_multi_f32(const float2* const* V, int k, float2* const* W, int nw, uin
     mdot_multi_f32_cuda(V, k, W, nw, n, out, ws, s);
 }
 
+// Row chunks for a grid of ncol columns on `slots` resident CTAs: the fewest
+// waves (from two) whose last wave is at least 90% full, at most g_max chunks
+// (every chunk a whole grid-stride sweep, so a nearly empty last wave costs a
+// full CTA time).
+static int balanced_chunks(int ncol, int slots, int g_max) {
+    for (int waves = 2; waves <= 16; ++waves) {
+        const int g = std::max(1, waves * slots / ncol);
+        if (g > g_max) break;
+        const long long total = (long long)g * ncol, full = (total + slots - 1) / slots;
+        if ((double)total >= 0.9 * (double)(full * slots)) return g;
+    }
+    return g_max;
+}
+
 void mdot_multi_f32_fast(const float2* const* V, int k, float2* const* W, int nw, uint64_t n, std::complex<double>* out,
                          Workspace& ws, cudaStream_t s) {
     if (k <= 0 || nw <= 0) return;
@@ -791,7 +805,7 @@ void mdot_multi_f32_fast(const float2* const* V, int k, float2* const* W, int nw
         const int ncol = (k + kc - 1) / kc;
         int per_sm = 1;
         QKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
-        g = std::min(g, std::max(1, 152 * std::max(1, per_sm) * 2 / ncol));
+        g = balanced_chunks(ncol, 152 * std::max(1, per_sm), g);
         kern<<<dim3(ncol, g), kThreads, 0, s>>>(V, k, dw, n, part, g);
     };
     switch (nw) {

@@ -187,7 +187,10 @@ def mdot(a):
     vals = {}
     for name, method in (("cuda", 0), ("tensor", 1), ("fast", 2)):
         call = lambda: qk.lib().qkrylov_vector_mdot_device_f32(va, k, wa, nw, n, method, out, stream)
-        for _ in range(3):
+        if call() != 0:  # a shape the kernel does not take (the tensor kernel: k <= 128)
+            res[name + "_us"] = None
+            continue
+        for _ in range(2):
             assert call() == 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -199,7 +202,8 @@ def mdot(a):
         res[name + "_GBs"] = round(res["bytes_per_call"] / t / 1e9, 1)
     big = max(map(abs, vals["cuda"]))
     for name in ("tensor", "fast"):
-        res[name + "_max_rel_diff"] = max(abs(x - y) for x, y in zip(vals["cuda"], vals[name])) / big
+        if name in vals:
+            res[name + "_max_rel_diff"] = max(abs(x - y) for x, y in zip(vals["cuda"], vals[name])) / big
     print(json.dumps(res), flush=True)
 
 
